@@ -598,6 +598,7 @@ char *es_o_scan(u64 lo, u64 hi, u64 M, const u64 *mods, const u64 *ress, size_t 
   o_ucert *uc; size_t nuc = es_o_gen_ucerts(UCERT_RMAX, UCERT_UMAX, &uc);
   o_wheel w = o_build_wheel(M, wc, nwc, uc, nuc);
   free(wc); free(uc);
+  td_init();                       /* once, before the lanes run in parallel */
   o_stats *lst = calloc(w.n, sizeof(o_stats));
   o_text *lem = calloc(w.n, sizeof(o_text));
 #ifdef _OPENMP
