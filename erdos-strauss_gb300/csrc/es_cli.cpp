@@ -1,0 +1,324 @@
+// es_cli.cpp -- rung_scan3_gb300: the reference scanner's command line over the GB300 engine.
+//
+// Same flags, refusals, exit codes and stdout record as sieve/rung_scan3.cpp:960-1163:
+//   rung_scan3_gb300 LO HI [--mmax N] [--wheel M] [--seg N] [--threads N] [--shard i/n]
+//                    [--progress N] [--filters FILE] [--sieve P] [--no-emit-survivors]
+//                    [--no-rung]   (cover_scan's test hook: skip stage D, exercise stage E)
+//   rung_scan3_gb300 --verify | --dump-classes [--wheel M] | --check-direct LO N
+//                    | --check-factor [N]
+// plus options of its own: --device N, --profile (stage timings on stderr), and
+//   rung_scan3_gb300 --batch FILE [flags]   one "LO HI" per line, each window's stream and
+//                                           SUMMARY in file order, run as one batch.
+// stdout carries only the certificate stream and SUMMARY; everything else goes to stderr.
+// Exit status: 0 no survivors, 2 survivors present, 1 refusal or error.
+#include "../../include/es_sieve.h"
+#include "es_wheel.h"
+
+#include <chrono>
+#include <cinttypes>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+typedef uint64_t u64;
+
+static void print_records(FILE *out, const es_record *r, size_t n, bool emit_surv) {
+  std::string buf;
+  buf.reserve(1 << 20);
+  char line[160];
+  for (size_t i = 0; i < n; ++i) {
+    if (!emit_surv && r[i].kind == ES_REC_SURVIVOR) continue;
+    const size_t k = es_format_record(&r[i], line, sizeof line);
+    buf.append(line, k);
+    if (buf.size() > (1 << 20)) { fwrite(buf.data(), 1, buf.size(), out); buf.clear(); }
+  }
+  fwrite(buf.data(), 1, buf.size(), out);
+}
+
+static int open_engine(es_config &cfg, es_engine **e) {
+  const es_status s = es_open(&cfg, e);
+  if (s == ES_OK) return 0;
+  if (s == ES_ERR_PIN) fprintf(stderr, "FATAL: %s\n", es_last_error(nullptr));
+  else fprintf(stderr, "FATAL: engine: %s (%s)\n", es_status_str(s), es_last_error(nullptr));
+  return 1;
+}
+
+static es_engine *default_engine(int device) {
+  es_config cfg{};
+  cfg.device = device;
+  es_engine *e = nullptr;
+  return open_engine(cfg, &e) ? nullptr : e;
+}
+
+// Walk the primes at or above lo on the device and run stage E on the first N
+// (sieve/rung_scan3.cpp:798-817). Certificates to stdout, status to stderr.
+static int check_direct(u64 lo, u64 N, int device) {
+  es_engine *e = default_engine(device);
+  if (!e) return 1;
+  std::vector<u64> primes;
+  const size_t chunk = 1 << 16;
+  std::vector<u64> cand(chunk);
+  std::vector<uint8_t> isp(chunk);
+  u64 p = lo | 1ull;
+  while (primes.size() < N) {
+    for (size_t i = 0; i < chunk; ++i) cand[i] = p + 2 * i;
+    if (es_is_prime_batch(e, cand.data(), chunk, isp.data()) != ES_OK) {
+      fprintf(stderr, "FATAL: %s\n", es_last_error(e)); es_close(e); return 1;
+    }
+    for (size_t i = 0; i < chunk && primes.size() < N; ++i) if (isp[i]) primes.push_back(cand[i]);
+    p += 2 * chunk;
+  }
+  std::vector<es_record> recs(N);
+  std::vector<uint8_t> found(N);
+  const es_status s = es_solve_direct_batch(e, primes.data(), N, recs.data(), found.data());
+  if (s != ES_OK) { fprintf(stderr, "FATAL: %s\n", es_last_error(e)); es_close(e); return 1; }
+  u64 solved = 0;
+  char line[160];
+  for (u64 i = 0; i < N; ++i) {
+    if (found[i]) { ++solved; es_format_record(&recs[i], line, sizeof line); fputs(line, stdout); }
+    else fprintf(stderr, "  stage E DECLINED p=%llu\n", (unsigned long long)primes[i]);
+  }
+  fprintf(stderr, "%s check-direct %llu/%llu primes at or above %llu solved by stage E (ceiling %llu)\n",
+          solved == N ? "ok  " : "FAIL", (unsigned long long)solved, (unsigned long long)N,
+          (unsigned long long)lo, (unsigned long long)es::DIRECT_PMAX);
+  es_close(e);
+  return solved == N ? 0 : 1;
+}
+
+// The adversarial factorization battery of sieve/rung_scan3.cpp:459-530, run on the device.
+// Independent of any second factorizer: every product of prime powers must give back n,
+// and every reported prime must pass the device Miller-Rabin.
+static int check_factor(u64 nper, int device) {
+  es_engine *e = default_engine(device);
+  if (!e) return 1;
+  u64 seed = 0x9e3779b97f4a7c15ull;
+  auto rnd = [&]() { seed ^= seed << 13; seed ^= seed >> 7; seed ^= seed << 17; return seed; };
+  auto next_prime = [&](u64 a) {   // smallest prime >= a, by device batches
+    std::vector<u64> c(256);
+    std::vector<uint8_t> f(256);
+    for (;;) {
+      for (int i = 0; i < 256; ++i) c[i] = a + (u64)i;
+      es_is_prime_batch(e, c.data(), 256, f.data());
+      for (int i = 0; i < 256; ++i) if (f[i]) return c[i];
+      a += 256;
+    }
+  };
+  const u64 NMAX = 18446744065119617025ull;
+  std::vector<u64> vals;
+  for (u64 dec = 1000000ull; dec < NMAX / 10; dec *= 10)
+    for (u64 i = 0; i < nper; ++i) vals.push_back(dec + rnd() % (9 * dec));
+  for (u64 i = 0; i < nper; ++i) {
+    const u64 a = next_prime(3037000000ull + rnd() % 1257000000ull);
+    const u64 b = next_prime(2147483648ull + rnd() % 2147000000ull);
+    if ((unsigned __int128)a * b <= NMAX) vals.push_back(a * b);
+  }
+  for (u64 i = 0; i < nper; ++i) {
+    const u64 a = next_prime(2147483648ull + rnd() % 2147000000ull);
+    vals.push_back(a * a);
+  }
+  for (u64 i = 0; i < nper; ++i) {
+    u64 v = 1;
+    while (v < NMAX / 65536) v *= 2 + rnd() % 65535;
+    vals.push_back(v);
+  }
+  for (u64 i = 0; i < nper / 4 + 1; ++i) vals.push_back(next_prime(((1ull << 62) + rnd() % (1ull << 62)) | 1ull));
+  const u64 B = 65536ull * 65536ull;
+  const u64 edge[] = {B - 1, B, B + 1, (1ull << 63) - 1, 1ull << 63, (1ull << 63) + 1, NMAX - 2, NMAX - 1, NMAX, 1, 2};
+  for (u64 v : edge) vals.push_back(v);
+  const size_t n = vals.size();
+  std::vector<u64> pr(n * 16);
+  std::vector<uint8_t> ex(n * 16), k(n);
+  if (es_factor_batch(e, vals.data(), n, pr.data(), ex.data(), k.data()) != ES_OK) {
+    fprintf(stderr, "FATAL: %s\n", es_last_error(e)); es_close(e); return 1;
+  }
+  std::vector<u64> facs;
+  for (size_t i = 0; i < n; ++i) for (int j = 0; j < k[i]; ++j) facs.push_back(pr[i * 16 + j]);
+  std::vector<uint8_t> fp(facs.size());
+  if (!facs.empty()) es_is_prime_batch(e, facs.data(), facs.size(), fp.data());
+  u64 bad_prod = 0, bad_prime = 0;
+  for (size_t i = 0; i < n; ++i) {
+    unsigned __int128 prod = 1;
+    for (int j = 0; j < k[i]; ++j)
+      for (int t = 0; t < ex[i * 16 + j]; ++t) prod *= pr[i * 16 + j];
+    if (prod != (unsigned __int128)vals[i]) ++bad_prod;
+  }
+  for (uint8_t f : fp) if (!f) ++bad_prime;
+  const u64 bad = bad_prod + bad_prime;
+  printf("%s check-factor %zu values -- bad products: %llu, composite factors: %llu\n", bad ? "FAIL" : "ok  ", n,
+         (unsigned long long)bad_prod, (unsigned long long)bad_prime);
+  es_close(e);
+  return bad ? 1 : 0;
+}
+
+static int self_test(int device) {
+  std::string log;
+  int fails = es::wheel_self_test(log);
+  fputs(log.c_str(), stdout);
+  // The device path: primality of known values, and one rung certificate.
+  es_engine *e = default_engine(device);
+  if (!e) { printf("  FAIL device engine\n"); ++fails; }
+  else {
+    const u64 v[6] = {2, 3037000493ull, 4611686018427387847ull, 18446744073709551557ull, 561, 3215031751ull};
+    const uint8_t want[6] = {1, 1, 1, 1, 0, 0};
+    uint8_t got[6] = {0};
+    const bool ok = es_is_prime_batch(e, v, 6, got) == ES_OK && !memcmp(got, want, 6);
+    printf(ok ? "  ok   device Miller-Rabin                 6\n" : "  FAIL device Miller-Rabin\n");
+    if (!ok) ++fails;
+    es_close(e);
+  }
+  printf(fails ? "\nSELF-TEST FAILED (%d checks)\n" : "\nSELF-TEST PASSED\n", fails);
+  return fails ? 1 : 0;
+}
+
+int main(int argc, char **argv) {
+  int device = 0;
+  for (int i = 1; i + 1 < argc; ++i) if (!strcmp(argv[i], "--device")) device = atoi(argv[i + 1]);
+  if (argc >= 2 && !strcmp(argv[1], "--verify")) return self_test(device);
+  if (argc >= 4 && !strcmp(argv[1], "--check-direct"))
+    return check_direct(strtoull(argv[2], 0, 10), strtoull(argv[3], 0, 10), device);
+  if (argc >= 2 && !strcmp(argv[1], "--check-factor"))
+    return check_factor(argc >= 3 && argv[2][0] != '-' ? strtoull(argv[2], 0, 10) : 2000, device);
+  if (argc >= 2 && !strcmp(argv[1], "--dump-classes")) {
+    u64 dm = 2042040;
+    for (int i = 2; i + 1 < argc; ++i) if (!strcmp(argv[i], "--wheel")) dm = strtoull(argv[i + 1], 0, 10);
+    fputs(es::class_table_text(dm).c_str(), stdout);
+    return 0;
+  }
+  const bool batch = argc >= 3 && !strcmp(argv[1], "--batch");
+  if (argc < 3) {
+    fprintf(stderr,
+            "usage: %s LO HI [--mmax N] [--wheel M] [--seg N] [--threads N]\n"
+            "                 [--shard i/n] [--progress N] [--filters FILE] [--sieve P]\n"
+            "                 [--no-emit-survivors] [--device N] [--profile]\n"
+            "       %s --batch FILE [flags]\n"
+            "       %s --verify | --dump-classes [--wheel M] | --check-direct LO N | --check-factor [N]\n"
+            "GB300 verification sieve: certifies 4/p solvable for every prime in [LO, HI),\n"
+            "byte for byte the record of the reference rung_scan3.\n",
+            argv[0], argv[0], argv[0]);
+    return 1;
+  }
+  u64 lo = 0, hi = 0;
+  if (!batch) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
+  u64 M = 2042040, mmax = 10000, seg = 262144, shard = 0, nshard = 1, sieve_p = 0;
+  bool emit_surv = true, profile = false, no_rung = false;
+  const char *ffile = nullptr;
+  for (int i = 3; i < argc; ++i) {
+    if (!strcmp(argv[i], "--mmax") && i + 1 < argc) mmax = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--wheel") && i + 1 < argc) M = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--seg") && i + 1 < argc) seg = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--progress") && i + 1 < argc) ++i;
+    else if (!strcmp(argv[i], "--threads") && i + 1 < argc) ++i;
+    else if (!strcmp(argv[i], "--device") && i + 1 < argc) ++i;
+    else if (!strcmp(argv[i], "--filters") && i + 1 < argc) ffile = argv[++i];
+    else if (!strcmp(argv[i], "--sieve") && i + 1 < argc) sieve_p = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--shard") && i + 1 < argc) {
+      unsigned long long a = 0, b = 1;
+      if (sscanf(argv[++i], "%llu/%llu", &a, &b) == 2) { shard = a; nshard = b; }
+    } else if (!strcmp(argv[i], "--no-emit-survivors")) emit_surv = false;
+    else if (!strcmp(argv[i], "--profile")) profile = true;
+    else if (!strcmp(argv[i], "--no-rung")) no_rung = true;
+    else { fprintf(stderr, "FATAL: unknown option '%s'\n", argv[i]); return 1; }
+  }
+  if (!seg) seg = 262144;
+  if (nshard == 0) nshard = 1;
+  if (!batch && nshard > 1) {                 // ceil-span tiling, sieve/rung_scan3.cpp:1022-1027
+    const u64 span = (hi - lo + nshard - 1) / nshard;
+    const u64 a = lo + shard * span, b = std::min(hi, a + span);
+    lo = a; hi = std::max(a, b);
+  }
+  uint64_t *fm = nullptr, *fr = nullptr;
+  size_t nfil = 0;
+  if (ffile) {
+    const es_status s = es_load_filters(ffile, &fm, &fr, &nfil);
+    if (s == ES_ERR_FILTERS) {
+      FILE *t = fopen(ffile, "r");
+      if (!t) fprintf(stderr, "FATAL: cannot open %s\n", ffile);
+      else { fclose(t); fprintf(stderr, "FATAL: no FILTER lines in %s\n", ffile); }
+      return 1;
+    }
+    if (s != ES_OK) { fprintf(stderr, "FATAL: %s\n", es_status_str(s)); return 1; }
+  }
+  es_config cfg{};
+  cfg.wheel_M = M; cfg.mmax = mmax; cfg.sieve_p = sieve_p; cfg.seg = seg;
+  cfg.filter_mods = fm; cfg.filter_ress = fr; cfg.n_filters = nfil; cfg.device = device;
+  cfg.flags = no_rung ? ES_FLAG_NO_RUNG : 0;
+  const auto t0 = std::chrono::steady_clock::now();
+  es_engine *e = nullptr;
+  if (open_engine(cfg, &e)) { es_free_u64(fm); es_free_u64(fr); return 1; }
+  es_free_u64(fm); es_free_u64(fr);
+  es_info_t info;
+  es_info(e, &info);
+  if (!info.pinned) fprintf(stderr, "[rung_scan3_gb300] WARNING: no pinned digest for M=%llu -- running UNPINNED\n",
+                            (unsigned long long)M);
+  std::vector<es_window> wins;
+  if (batch) {
+    FILE *fp = fopen(argv[2], "r");
+    if (!fp) { fprintf(stderr, "FATAL: cannot open %s\n", argv[2]); es_close(e); return 1; }
+    unsigned long long a, b;
+    while (fscanf(fp, "%llu %llu", &a, &b) == 2) wins.push_back({a, b});
+    fclose(fp);
+  } else {
+    wins.push_back({lo, hi});
+  }
+  for (const es_window &w : wins) {
+    if (w.hi > info.ceiling) {
+      fprintf(stderr, "FATAL: HI must not exceed %llu, the stage-E ceiling: above it isqrt_u64 in the frozen "
+                      "reference overflows, and a prime stage D misses would be reported as a survivor rather "
+                      "than solved\n", (unsigned long long)info.ceiling);
+      es_close(e);
+      return 1;
+    }
+    if (w.lo <= info.floor) {
+      fprintf(stderr, "FATAL: LO must exceed max pmin of the filter table (%llu); the region below is settled "
+                      "by the existing censuses\n", (unsigned long long)info.floor);
+      es_close(e);
+      return 1;
+    }
+  }
+  fprintf(stderr,
+          "[rung_scan3_gb300] wheel M=%llu lanes=%llu (spacing %.0f)  covers=%llu (mmax=%llu)  seg=%llu  "
+          "wheel_pmin=%llu\n[rung_scan3_gb300] filters=%llu fnv64=%016llx source=%s sieve=%llu (+%llu primes)\n",
+          (unsigned long long)M, (unsigned long long)info.lanes, (double)M / (double)info.lanes,
+          (unsigned long long)info.n_certified, (unsigned long long)mmax, (unsigned long long)seg,
+          (unsigned long long)info.wheel_pmin, (unsigned long long)info.n_certified,
+          (unsigned long long)info.filter_fnv64, ffile ? ffile : "generated", (unsigned long long)sieve_p,
+          (unsigned long long)(info.n_filters - info.n_certified));
+  const auto t1 = std::chrono::steady_clock::now();
+  std::vector<es_counters> cnt(wins.size());
+  es_records recs{};
+  const es_status s = wins.size() == 1 ? es_run_window(e, wins[0].lo, wins[0].hi, &cnt[0], &recs)
+                                       : es_run_batch(e, wins.data(), wins.size(), ES_SCHED_PERSISTENT, cnt.data(), &recs);
+  if (s != ES_OK) {
+    fprintf(stderr, "FATAL: %s: %s\n", es_status_str(s), es_last_error(e));
+    es_close(e);
+    return 1;
+  }
+  const auto t2 = std::chrono::steady_clock::now();
+  u64 survivors = 0;
+  size_t r0 = 0;
+  for (size_t w = 0; w < wins.size(); ++w) {
+    size_t r1 = r0;
+    while (r1 < recs.n && recs.recs[r1].window == w) ++r1;
+    print_records(stdout, recs.recs + r0, r1 - r0, emit_surv);
+    char line[512];
+    fputs(es_format_summary(e, wins[w].lo, wins[w].hi, &cnt[w], line, sizeof line) ? line : "SUMMARY ?\n", stdout);
+    survivors += cnt[w].survivors;
+    r0 = r1;
+  }
+  fflush(stdout);
+  if (profile) {
+    es_timing_t t;
+    es_timing(e, &t);
+    fprintf(stderr,
+            "[profile] setup=%.3fs run=%.3fs device_total=%.3fms mark=%.3fms mr=%.3fms rung=%.3fms direct=%.3fms "
+            "items=%llu survivors=%llu primes=%llu launches=%llu\n",
+            std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count(),
+            t.total_ms, t.mark_ms, t.mr_ms, t.rung_ms, t.direct_ms, (unsigned long long)t.mark_items,
+            (unsigned long long)t.survivors, (unsigned long long)t.primes, (unsigned long long)t.kernel_launches);
+  }
+  es_free_records(&recs);
+  es_close(e);
+  return survivors ? 2 : 0;
+}

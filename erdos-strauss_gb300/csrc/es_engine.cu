@@ -1,0 +1,977 @@
+// es_engine.cu -- the GB300 engine: device tables, the funnel kernels, and the C ABI.
+//
+// Data layout in HBM (resident for the engine's lifetime):
+//   rho[L]            u32  lane classes mod M in wheel order
+//   K0[L][ldk]        u16  per (lane, filter): the residue K0 = K mod s at which filter f
+//                          kills lane l (p = rho_l + M*K), or K0_MISS; 2308 x 3752 x 2 B
+//                          = 17.3 MB for the M = 2042040 table, read coalesced row by row
+//   fdesc[nf], sdist  u32  stride s = mod/gcd(M,mod) per filter, and the distinct strides
+//   tdp/tde                trial-division table: 6541 odd primes < 2^16 with inverses
+// Per run: window descriptors, the survivor list, prime/direct index lists, records.
+//
+// Pipeline per run (one CUDA stream):
+//   k_mark    one CTA per (window, lane, segment) item: a byte per position in shared
+//             memory, each filter clears its progression j = off, off+s, ... (plain byte
+//             stores: clearing is idempotent, so no atomics), popcount, warp-aggregated
+//             compaction of survivors (ballot/popc prefix) into the survivor list
+//   k_mr      one thread per survivor: base-2 SPRP then the 12-base Miller-Rabin
+//   k_rung    one thread per prime: the rung walk with device factorization
+//   k_direct  one thread per prime left over: the direct search, else SURVIVOR
+// Records come back unordered and the host sorts them by (window, lane, J): the
+// reference's lane-major order per window.
+#include "../../include/es_sieve.h"
+#include "es_arith.cuh"
+#include "es_kernels.cuh"
+#include "es_wheel.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cinttypes>
+#include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace es {
+
+// ============================================================================ kernels
+
+// K0 table: for lane l and filter f, p = rho + M*K == res (mod mod) iff
+// g | (res - rho) and K == ((res - rho) mod mod)/g * inv((M/g) mod s, s) (mod s).
+// This is the per-(lane, filter) setup of sieve/rung_scan3.cpp:719-728 moved from the
+// window's first position to K = 0, so it no longer depends on the window at all.
+__global__ void k_build_k0(const u32 *__restrict__ rho, u32 L, const u64 *__restrict__ mods,
+                           const u64 *__restrict__ ress, const u32 *__restrict__ gs,
+                           const u32 *__restrict__ invs, const u32 *__restrict__ fdesc, u32 nf,
+                           u32 ldk, u16 *__restrict__ K0) {
+  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (u64)L * ldk) return;
+  const u32 l = (u32)(idx / ldk), f = (u32)(idx % ldk);
+  if (f >= nf) { K0[idx] = K0_MISS; return; }
+  const u64 mod = mods[f];
+  const u64 d = (ress[f] % mod + mod - rho[l] % mod) % mod;
+  const u32 g = gs[f], s = fdesc[f] & 0xFFFFu;
+  if (d % g) { K0[idx] = K0_MISS; return; }
+  K0[idx] = (u16)((d / g) * (u64)invs[f] % s);
+}
+
+// Clear the progression of every filter in [from, to) over alive[0, n).
+template <int BLOCK>
+__device__ __forceinline__ void mark_filters(const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
+                                             const u16 *R, unsigned char *alive, u32 from, u32 to, u32 n) {
+  for (u32 f = from + threadIdx.x; f < to; f += BLOCK) {
+    const u32 k0 = K0row[f];
+    if (k0 == K0_MISS) continue;
+    const u32 fd = __ldg(fdesc + f);
+    const u32 s = fd & 0xFFFFu;
+    int off = (int)k0 - (int)R[fd >> 16];
+    if (off < 0) off += (int)s;
+    for (u32 j = (u32)off; j < n; j += s) alive[j] = 0;
+  }
+}
+
+template <int BLOCK>
+__device__ __forceinline__ u32 block_sum(u32 v, u32 *red) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  __syncthreads();
+  if (ln == 0) red[wid] = v;
+  __syncthreads();
+  u32 t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < BLOCK / 32 ? red[threadIdx.x] : 0;
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+  }
+  return t;   // valid in thread 0
+}
+
+struct ItemInfo {
+  u64 first, Kb;     // first position p of the lane in the window; K of the segment start
+  u64 J0;            // position index of the segment start within the lane
+  u32 n, lane, win, valid;
+};
+
+// Items are dealt from an atomic queue (persistent schedule: gridDim = resident CTAs) or
+// one per CTA (gridDim = items). Item i of window w covers lane (i - item0) % L, segment
+// (i - item0) / L.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persistent) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  u16 *R = reinterpret_cast<u16 *>(smem);
+  unsigned char *alive = smem + P.r_bytes;
+  u32 *alive32 = reinterpret_cast<u32 *>(alive);
+  __shared__ ItemInfo it;
+  __shared__ u32 red[BLOCK / 32];
+  __shared__ u64 s_item;
+  const u32 lane_id = threadIdx.x & 31;
+  u64 next = blockIdx.x;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const u64 item = persistent ? atomicAdd(reinterpret_cast<unsigned long long *>(P.queue), 1ull) : next;
+      s_item = item;
+      it.valid = 0;
+      if (item < P.total_items) {
+        u32 lo = 0, hi = P.nwin;                   // last window with item0 <= item
+        while (hi - lo > 1) {
+          const u32 mid = (lo + hi) >> 1;
+          if (P.win[mid].item0 <= item) lo = mid; else hi = mid;
+        }
+        const WinDev W = P.win[lo];
+        const u64 rem = item - W.item0;
+        const u32 lane = (u32)(rem % P.L);
+        const u64 seg = rem / P.L;
+        const u64 rho = P.rho[lane];
+        const u64 Kfirst = W.Q + (rho < W.lomod ? 1 : 0);
+        const u64 first = rho + P.M * Kfirst;
+        if (first < W.hi) {
+          const u64 npos = (W.hi - first - 1) / P.M + 1;
+          const u64 J0 = seg * P.seg;
+          if (J0 < npos) {
+            it.first = first;
+            it.J0 = J0;
+            it.Kb = Kfirst + J0;
+            it.n = (u32)min((u64)P.seg, npos - J0);
+            it.lane = lane;
+            it.win = lo;
+            it.valid = 1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const u64 item = s_item;
+    if (item >= P.total_items) break;
+    next += gridDim.x;
+    if (!it.valid) { __syncthreads(); continue; }
+    const u32 n = it.n, lane = it.lane, win = it.win;
+    const u64 Kb = it.Kb;
+    // Residue of the segment's first K modulo every distinct stride.
+    for (u32 d = threadIdx.x; d < P.D; d += BLOCK) R[d] = (u16)(Kb % P.sdist[d]);
+    const u32 nw = (n + 3) >> 2;
+    for (u32 w = threadIdx.x; w < nw; w += BLOCK) {
+      const u32 left = n - 4 * w;
+      alive32[w] = left >= 4 ? 0x01010101u : (0x01010101u & ((1u << (8 * left)) - 1u));
+    }
+    __syncthreads();
+    const u16 *K0row = P.K0 + (size_t)lane * P.ldk;
+    mark_filters<BLOCK>(K0row, P.fdesc, R, alive, 0, P.ncov, n);      // stage B: covers
+    __syncthreads();
+    if (P.nf > P.ncov) {                                               // stage B': primes
+      u32 c = 0;
+      for (u32 w = threadIdx.x; w < nw; w += BLOCK) c += __popc(alive32[w]);
+      c = block_sum<BLOCK>(c, red);
+      if (threadIdx.x == 0) atomicAdd(&P.cnt[win].after_covers, (unsigned long long)c);
+      mark_filters<BLOCK>(K0row, P.fdesc, R, alive, P.ncov, P.nf, n);
+      __syncthreads();
+    }
+    // Compaction: each warp takes 32 consecutive words per step; an inclusive warp scan of
+    // the per-word popcounts gives each lane its slot, and one atomicAdd per warp reserves
+    // the warp's block in the survivor list.
+    u32 mine = 0;
+    const u32 wid = threadIdx.x >> 5;
+    for (u32 base = wid * 32; base < nw; base += BLOCK) {
+      const u32 w = base + lane_id;
+      u32 x = w < nw ? alive32[w] : 0u;
+      const u32 c = __popc(x);
+      u32 incl = c;
+      #pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane_id >= (u32)o) incl += t;
+      }
+      const u32 tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      if (tot) {
+        unsigned long long gbase = 0;
+        if (lane_id == 0) gbase = atomicAdd(P.surv_count, (unsigned long long)tot);
+        gbase = __shfl_sync(0xFFFFFFFFu, gbase, 0);
+        u64 slot = gbase + incl - c;
+        while (x) {
+          const u32 k = __ffs(x) - 1;
+          x &= x - 1;
+          if (slot < P.surv_cap) {
+            const u64 J = it.J0 + 4ull * w + (k >> 3);
+            Surv s;
+            s.p = it.first + P.M * J;
+            s.J = J;
+            s.win = win;
+            s.lane = lane;
+            P.surv[slot] = s;
+          }
+          ++slot;
+        }
+        mine += tot;
+      }
+    }
+    // `mine` is the same in every lane of a warp: lane 0 adds it once.
+    if (lane_id == 0 && mine) atomicAdd(&P.cnt[win].surv, (unsigned long long)mine);
+    if (threadIdx.x == 0) atomicAdd(&P.cnt[win].positions, (unsigned long long)n);
+    __syncthreads();
+  }
+}
+
+__global__ void k_mr(const TailParams T) {
+  const u64 n = min((u64)*T.surv_count, T.cap);
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const Surv s = T.surv[i];
+    if (sprp2_64(s.p) && is_prime64(s.p)) {
+      const unsigned long long k = atomicAdd(T.prime_count, 1ull);
+      if (k < T.cap) T.primes[k] = (u32)i;
+    } else {
+      atomicAdd(&T.cnt[s.win].composite, 1ull);
+    }
+  }
+}
+
+__device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r) {
+  const unsigned long long k = atomicAdd(T.rec_count, 1ull);
+  if (k < T.cap) T.recs[k] = r;
+}
+
+__global__ void k_rung(const TailParams T, int no_rung) {
+  const u64 n = min((u64)*T.prime_count, T.cap);
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const u32 si = T.primes[i];
+    const Surv s = T.surv[si];
+    u64 A; u32 r; U128 u;
+    if (!no_rung && solve_rung(s.p, A, r, u, T.tdp, T.tde, T.status)) {
+      RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, A, r, u.lo, u.hi};
+      put_record(T, rec);
+      atomicAdd(&T.cnt[s.win].rung, 1ull);
+    } else {
+      const unsigned long long k = atomicAdd(T.direct_count, 1ull);
+      if (k < T.cap) T.direct[k] = si;
+    }
+  }
+}
+
+__global__ void k_direct(const TailParams T) {
+  const u64 n = min((u64)*T.direct_count, T.cap);
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const Surv s = T.surv[T.direct[i]];
+    u64 a, c, d, k;
+    if (solve_direct(s.p, a, c, d, k, T.tdp, T.tde, T.status)) {
+      RecDev rec{ES_REC_SOLVED, s.win, s.lane, 0, s.J, s.p, a, c, d, k};
+      put_record(T, rec);
+      atomicAdd(&T.cnt[s.win].direct, 1ull);
+    } else {
+      RecDev rec{ES_REC_SURVIVOR, s.win, s.lane, 0, s.J, s.p, 0, 0, 0, 0};
+      put_record(T, rec);
+      atomicAdd(&T.cnt[s.win].unsolved, 1ull);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- probe kernels
+__global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x)
+    out[i] = (sprp2_64(n[i]) && is_prime64(n[i])) ? 1 : 0;
+}
+__global__ void k_probe_rung(const u64 *p, u64 count, RecDev *out, unsigned char *found,
+                             const u32 *tdp, const TdEntry *tde, u32 *status) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
+    u64 A; u32 r; U128 u;
+    const bool ok = solve_rung(p[i], A, r, u, tdp, tde, status);
+    found[i] = ok;
+    out[i] = ok ? RecDev{ES_REC_RUNG, 0, 0, 0, 0, p[i], A, r, u.lo, u.hi} : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
+  }
+}
+__global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned char *found,
+                               const u32 *tdp, const TdEntry *tde, u32 *status) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
+    u64 a, c, d, k;
+    const bool ok = solve_direct(p[i], a, c, d, k, tdp, tde, status);
+    found[i] = ok;
+    out[i] = ok ? RecDev{ES_REC_SOLVED, 0, 0, 0, 0, p[i], a, c, d, k} : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
+  }
+}
+__global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *ex, unsigned char *k,
+                               const u32 *tdp, const TdEntry *tde, u32 *status) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
+    Fac f;
+    if (!factor64(n[i], f, tdp, tde, status)) f.k = 0;
+    for (int a = 1; a < f.k; ++a)                       // ascending primes
+      for (int b = a; b > 0 && f.pr[b - 1] > f.pr[b]; --b) {
+        const u64 t = f.pr[b]; f.pr[b] = f.pr[b - 1]; f.pr[b - 1] = t;
+        const unsigned char e = f.ex[b]; f.ex[b] = f.ex[b - 1]; f.ex[b - 1] = e;
+      }
+    for (int a = 0; a < MAXF; ++a) {
+      pr[i * MAXF + a] = a < f.k ? f.pr[a] : 0;
+      ex[i * MAXF + a] = a < f.k ? f.ex[a] : 0;
+    }
+    k[i] = (unsigned char)f.k;
+  }
+}
+
+// ============================================================================ host engine
+
+constexpr int MARK_BLOCK = 128;
+constexpr u32 DEFAULT_SEG = 16384;        // positions per marking item (bytes of shared memory)
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace es
+
+struct es_engine {
+  // configuration and derived tables
+  es::u64 M = 0, mmax = 0, sieve_p = 0;
+  uint32_t flags = 0;
+  std::vector<es::u64> classes;
+  es::u64 wheel_pmin = 0, cover_pmax = 0, class_fnv = 0, filter_fnv = 0;
+  const es::ClassPin *pin = nullptr;
+  std::vector<es::u64> mods, ress;     // certified filters [0,ncov) then stage-B' primes
+  size_t ncov = 0;
+  // marking order: filters sorted by stride within each phase
+  std::vector<uint32_t> order;
+  uint32_t nf = 0, ldk = 0, D = 0, seg = es::DEFAULT_SEG;
+  int device = 0, sm_count = 0, mark_occupancy = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  // resident device tables
+  es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
+  es::u16 *d_K0 = nullptr;
+  es::TdEntry *d_tde = nullptr;
+  // per-run buffers
+  es::WinDev *d_win = nullptr; size_t win_cap = 0;
+  es::WinCount *d_cnt = nullptr;
+  es::Surv *d_surv = nullptr;
+  es::u32 *d_primes = nullptr, *d_direct = nullptr;
+  es::RecDev *d_recs = nullptr;
+  size_t cap = 0;
+  unsigned long long *d_ctr = nullptr;   // [0] queue [1] surv [2] prime [3] direct [4] rec
+  es::u32 *d_status = nullptr;
+  es_timing_t timing{};
+  std::string last_error;
+  std::mutex mu;                         // serialises device work on this engine
+};
+
+namespace es {
+
+static es_status fail(es_engine *e, es_status s, const std::string &msg) {
+  if (e) e->last_error = msg;
+  return s;
+}
+
+#define CU(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t err_ = (call);                                                             \
+    if (err_ != cudaSuccess)                                                               \
+      return fail(e, ES_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));   \
+  } while (0)
+
+static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
+  if (nwin > e->win_cap) {
+    if (e->d_win) cudaFree(e->d_win);
+    if (e->d_cnt) cudaFree(e->d_cnt);
+    e->d_win = nullptr; e->d_cnt = nullptr;
+    size_t want = std::max<size_t>(nwin, 64);
+    CU(cudaMalloc(&e->d_win, want * sizeof(WinDev)));
+    CU(cudaMalloc(&e->d_cnt, want * sizeof(WinCount)));
+    e->win_cap = want;
+  }
+  if (cap > e->cap) {
+    cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
+    e->d_surv = nullptr; e->d_primes = e->d_direct = nullptr; e->d_recs = nullptr;
+    CU(cudaMalloc(&e->d_surv, cap * sizeof(Surv)));
+    CU(cudaMalloc(&e->d_primes, cap * sizeof(u32)));
+    CU(cudaMalloc(&e->d_direct, cap * sizeof(u32)));
+    CU(cudaMalloc(&e->d_recs, cap * sizeof(RecDev)));
+    e->cap = cap;
+  }
+  return ES_OK;
+}
+
+static MarkParams mark_params(const es_engine *e, u64 total_items, u32 nwin) {
+  MarkParams P;
+  P.rho = e->d_rho; P.K0 = e->d_K0; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
+  P.win = e->d_win; P.queue = reinterpret_cast<u64 *>(e->d_ctr + 0);
+  P.surv = e->d_surv; P.surv_count = e->d_ctr + 1; P.cnt = e->d_cnt;
+  P.total_items = total_items; P.surv_cap = e->cap; P.M = e->M;
+  P.L = (u32)e->classes.size(); P.ldk = e->ldk; P.nf = e->nf; P.ncov = (u32)e->ncov;
+  P.D = e->D; P.nwin = nwin; P.seg = e->seg;
+  P.r_bytes = (2 * e->D + 15) & ~15u;
+  return P;
+}
+
+static TailParams tail_params(const es_engine *e) {
+  TailParams T;
+  T.surv = e->d_surv; T.surv_count = e->d_ctr + 1;
+  T.primes = e->d_primes; T.prime_count = e->d_ctr + 2;
+  T.direct = e->d_direct; T.direct_count = e->d_ctr + 3;
+  T.recs = e->d_recs; T.rec_count = e->d_ctr + 4;
+  T.cnt = e->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = e->d_status;
+  T.cap = e->cap;
+  return T;
+}
+
+static size_t mark_smem(const es_engine *e) { return ((2 * e->D + 15) & ~15u) + e->seg + 16; }
+
+// Window descriptors and their item offsets (lanes x segments per window).
+static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vector<WinDev> &out) {
+  out.resize(n);
+  u64 items = 0;
+  const u64 L = e->classes.size();
+  for (size_t i = 0; i < n; ++i) {
+    WinDev &d = out[i];
+    d.lo = w[i].lo; d.hi = std::max(w[i].lo, w[i].hi);
+    d.Q = d.lo / e->M;
+    d.lomod = (u32)(d.lo % e->M);
+    const u64 len = d.hi - d.lo;
+    const u64 maxpos = len ? (len - 1) / e->M + 1 : 0;     // most positions any lane can hold
+    d.nseg = (u32)((maxpos + e->seg - 1) / e->seg);
+    d.item0 = items;
+    items += (u64)d.nseg * L;
+  }
+  return items;
+}
+
+// One pass of the funnel over the windows described in d_win, counting into cnt.
+// `persistent` selects the queue-driven k_mark (grid = resident CTAs); otherwise one CTA
+// per item.
+static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool persistent, WinCount *cnt) {
+  MarkParams P = mark_params(e, total_items, nwin);
+  TailParams T = tail_params(e);
+  P.cnt = cnt;
+  T.cnt = cnt;
+  const size_t smem = mark_smem(e);
+  CU(cudaMemsetAsync(e->d_ctr, 0, 8 * sizeof(unsigned long long), e->stream));
+  unsigned grid = persistent ? (unsigned)std::min<u64>(total_items, (u64)e->sm_count * e->mark_occupancy)
+                             : (unsigned)std::min<u64>(total_items, 0x7FFFFFFFull);
+  if (grid == 0) grid = 1;
+  CU(cudaEventRecord(e->ev[0], e->stream));
+  k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, smem, e->stream>>>(P, persistent ? 1 : 0);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(e->ev[1], e->stream));
+  k_mr<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(e->ev[2], e->stream));
+  k_rung<<<e->sm_count * 4, 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(e->ev[3], e->stream));
+  k_direct<<<e->sm_count, 32, 0, e->stream>>>(T);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(e->ev[4], e->stream));
+  return ES_OK;
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+static std::string status_text(u32 st) {
+  std::string s;
+  if (st & ST_RHO_BUDGET) s += " rho-budget";
+  if (st & ST_FAC_OVERFLOW) s += " factor-overflow";
+  if (st & ST_STACK_OVERFLOW) s += " factor-stack";
+  if (st & ST_QUEUE_TIMEOUT) s += " queue-timeout";
+  if (st & ST_BAD_INPUT) s += " bad-input";
+  return s;
+}
+
+// Runs windows through the funnel and collects counters and sorted records. Re-runs
+// with larger buffers when the survivor list overflowed (the count is exact even then).
+static es_status run_windows(es_engine *e, const es_window *w, size_t n, int schedule,
+                             es_counters *per_window, es_records *recs) {
+  const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
+  for (size_t i = 0; i < n; ++i) {
+    if (w[i].hi > DIRECT_PMAX)
+      return fail(e, ES_ERR_RANGE, "HI must not exceed the stage-E ceiling " + std::to_string(DIRECT_PMAX));
+    if (w[i].lo <= floor_)
+      return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
+  }
+  std::vector<WinDev> wd;
+  const u64 total_items = describe(e, w, n, wd);
+  u64 positions_bound = 0;
+  for (const WinDev &d : wd) positions_bound += (u64)d.nseg * e->seg * e->classes.size();
+  size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
+  cap = std::max(cap, e->cap);
+  const bool one_pass = schedule == ES_SCHED_PERSISTENT || n == 1;
+  std::vector<WinCount> hc(n);
+  std::vector<RecDev> hr;
+  bool done = false;
+  for (int attempt = 0; attempt < 4 && !done; ++attempt) {
+    es_status s = ensure_capacity(e, n, cap);
+    if (s) return s;
+    CU(cudaMemsetAsync(e->d_cnt, 0, n * sizeof(WinCount), e->stream));
+    CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), e->stream));
+    unsigned long long ctr[8] = {0};
+    double mark_ms = 0, mr_ms = 0, rung_ms = 0, direct_ms = 0;
+    u64 launches = 0, surv_max = 0, surv_total = 0, prime_total = 0;
+    hr.clear();
+    CU(cudaEventRecord(e->ev[5], e->stream));
+    for (size_t i = 0; i < (one_pass ? 1 : n); ++i) {
+      // Plain schedule: the same kernels, one launch sequence per window.
+      WinDev one = wd[i];
+      one.item0 = 0;
+      const u64 items = one_pass ? total_items : (u64)one.nseg * e->classes.size();
+      CU(cudaMemcpyAsync(e->d_win, one_pass ? wd.data() : &one, (one_pass ? n : 1) * sizeof(WinDev),
+                         cudaMemcpyHostToDevice, e->stream));
+      s = launch_funnel(e, items, one_pass ? (u32)n : 1, schedule == ES_SCHED_PERSISTENT, e->d_cnt + (one_pass ? 0 : i));
+      if (s) return s;
+      launches += 4;
+      CU(cudaMemcpyAsync(ctr, e->d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, e->stream));
+      CU(cudaStreamSynchronize(e->stream));
+      mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
+      rung_ms += ev_ms(e->ev[2], e->ev[3]); direct_ms += ev_ms(e->ev[3], e->ev[4]);
+      surv_max = std::max<u64>(surv_max, ctr[1]);
+      surv_total += ctr[1]; prime_total += ctr[2];
+      if (ctr[1] > e->cap) break;
+      const size_t base = hr.size();
+      hr.resize(base + ctr[4]);
+      if (ctr[4]) CU(cudaMemcpy(hr.data() + base, e->d_recs, ctr[4] * sizeof(RecDev), cudaMemcpyDeviceToHost));
+      if (!one_pass) for (size_t k = base; k < hr.size(); ++k) hr[k].win = (u32)i;
+    }
+    CU(cudaEventRecord(e->ev[6], e->stream));
+    CU(cudaStreamSynchronize(e->stream));
+    if (surv_max > e->cap) {            // overflow: grow to the exact need and re-run
+      cap = (size_t)(surv_max + surv_max / 4 + 1024);
+      continue;
+    }
+    u32 st = 0;
+    CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
+    CU(cudaMemcpy(hc.data(), e->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost));
+    e->timing.total_ms = ev_ms(e->ev[5], e->ev[6]);
+    e->timing.mark_ms = mark_ms; e->timing.mr_ms = mr_ms;
+    e->timing.rung_ms = rung_ms; e->timing.direct_ms = direct_ms;
+    e->timing.marks_kernel_launches = one_pass ? 1 : n;
+    e->timing.kernel_launches = launches;
+    e->timing.mark_items = total_items;
+    e->timing.survivors = surv_total;
+    e->timing.primes = prime_total;
+    done = true;
+  }
+  if (!done) return fail(e, ES_ERR_NOMEM, "survivor list kept overflowing");
+  for (size_t i = 0; i < n; ++i) {      // the SUMMARY counters (sieve/rung_scan3.cpp:764-772)
+    const WinCount &c = hc[i];
+    es_counters &o = per_window[i];
+    o.positions = c.positions;
+    if (e->nf == e->ncov) { o.covered = c.positions - c.surv; o.sieved = 0; }
+    else { o.covered = c.positions - c.after_covers; o.sieved = c.after_covers - c.surv; }
+    o.mr = c.surv; o.composite = c.composite; o.rung = c.rung; o.direct = c.direct;
+    o.survivors = c.unsolved;
+  }
+  if (recs) {
+    std::sort(hr.begin(), hr.end(), [](const RecDev &a, const RecDev &b) {
+      if (a.win != b.win) return a.win < b.win;
+      if (a.lane != b.lane) return a.lane < b.lane;
+      return a.J < b.J;
+    });
+    recs->n = hr.size();
+    recs->recs = (es_record *)malloc(std::max<size_t>(hr.size(), 1) * sizeof(es_record));
+    if (!recs->recs) return fail(e, ES_ERR_NOMEM, "host records");
+    static_assert(sizeof(RecDev) == sizeof(es_record), "record layout");
+    memcpy(recs->recs, hr.data(), hr.size() * sizeof(es_record));
+  }
+  return ES_OK;
+}
+
+static es_status build_tables(es_engine *e) {
+  const u64 M = e->M;
+  const u32 L = (u32)e->classes.size();
+  const size_t nf = e->mods.size();
+  // Per filter: g = gcd(M, mod), s = mod/g, inv = ((M/g) mod s)^-1 mod s.
+  std::vector<u32> g(nf), s(nf), inv(nf);
+  for (size_t i = 0; i < nf; ++i) {
+    const u64 mod = e->mods[i];
+    if (mod == 0) return fail(e, ES_ERR_FILTERS, "filter with modulus 0");
+    if (mod > 0xFFFFFFFFull) return fail(e, ES_ERR_ARG, "filter modulus above 2^32 is not supported");
+    const u64 gg = gcd_u64(M, mod), ss = mod / gg;
+    if (ss > 0xFFFFull) return fail(e, ES_ERR_ARG, "filter stride mod/gcd(M,mod) above 65535 is not supported");
+    bool ok;
+    const u64 iv = ss == 1 ? 0 : inv_mod((M / gg) % ss, ss, ok);
+    if (ss != 1 && !ok) return fail(e, ES_ERR_ARG, "non-invertible stride (impossible for g = gcd)");
+    g[i] = (u32)gg; s[i] = (u32)ss; inv[i] = (u32)iv;
+  }
+  // Marking order: by stride within each phase, so that a warp's 32 filters have similar
+  // trip counts. Marking is idempotent, so the order cannot change the result.
+  e->order.resize(nf);
+  for (size_t i = 0; i < nf; ++i) e->order[i] = (u32)i;
+  std::stable_sort(e->order.begin(), e->order.begin() + e->ncov, [&](u32 a, u32 b) { return s[a] < s[b]; });
+  std::stable_sort(e->order.begin() + e->ncov, e->order.end(), [&](u32 a, u32 b) { return s[a] < s[b]; });
+  std::vector<u32> sd;
+  for (size_t i = 0; i < nf; ++i) sd.push_back(s[i]);
+  std::sort(sd.begin(), sd.end());
+  sd.erase(std::unique(sd.begin(), sd.end()), sd.end());
+  if (sd.size() > (size_t)DMAX) return fail(e, ES_ERR_ARG, "more than 8192 distinct filter strides");
+  e->D = (u32)sd.size();
+  std::vector<u64> om(nf), orr(nf);
+  std::vector<u32> og(nf), oinv(nf), fdesc(nf);
+  for (size_t k = 0; k < nf; ++k) {
+    const u32 i = e->order[k];
+    om[k] = e->mods[i]; orr[k] = e->ress[i]; og[k] = g[i]; oinv[k] = inv[i];
+    const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), s[i]) - sd.begin());
+    fdesc[k] = s[i] | (di << 16);
+  }
+  e->nf = (u32)nf;
+  e->ldk = (u32)((nf + 7) & ~7ull);
+  std::vector<u32> rho(L);
+  for (u32 l = 0; l < L; ++l) rho[l] = (u32)e->classes[l];
+  // trial-division table
+  std::vector<u32> tdp;
+  std::vector<TdEntry> tde;
+  {
+    std::vector<uint8_t> comp(65537, 0);
+    for (u64 i = 2; i <= 65536; ++i) {
+      if (comp[i]) continue;
+      for (u64 j = i * i; j <= 65536; j += i) comp[j] = 1;
+      if (i == 2) continue;
+      u64 x = i;
+      for (int k = 0; k < 5; ++k) x *= 2 - i * x;
+      tdp.push_back((u32)i);
+      tde.push_back(TdEntry{x, ~0ull / i});
+    }
+    if ((int)tdp.size() != NTD) return fail(e, ES_ERR_ARG, "trial-division table size");
+  }
+  u64 *d_mods = nullptr, *d_ress = nullptr;
+  u32 *d_g = nullptr, *d_inv = nullptr;
+  CU(cudaMalloc(&e->d_rho, L * sizeof(u32)));
+  CU(cudaMalloc(&e->d_fdesc, std::max<size_t>(nf, 1) * sizeof(u32)));
+  CU(cudaMalloc(&e->d_sdist, std::max<size_t>(sd.size(), 1) * sizeof(u32)));
+  CU(cudaMalloc(&e->d_K0, (size_t)L * e->ldk * sizeof(u16)));
+  CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
+  CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
+  CU(cudaMalloc(&e->d_ctr, 8 * sizeof(unsigned long long)));
+  CU(cudaMalloc(&e->d_status, sizeof(u32)));
+  CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
+  CU(cudaMalloc(&d_ress, std::max<size_t>(nf, 1) * sizeof(u64)));
+  CU(cudaMalloc(&d_g, std::max<size_t>(nf, 1) * sizeof(u32)));
+  CU(cudaMalloc(&d_inv, std::max<size_t>(nf, 1) * sizeof(u32)));
+  CU(cudaMemcpy(e->d_rho, rho.data(), L * sizeof(u32), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(e->d_fdesc, fdesc.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(e->d_sdist, sd.data(), sd.size() * sizeof(u32), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(e->d_tdp, tdp.data(), tdp.size() * sizeof(u32), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(e->d_tde, tde.data(), tde.size() * sizeof(TdEntry), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(d_mods, om.data(), nf * sizeof(u64), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(d_ress, orr.data(), nf * sizeof(u64), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(d_inv, oinv.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
+  const u64 total = (u64)L * e->ldk;
+  k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
+                                                                       e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(e->stream));
+  cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
+  // occupancy of the marking kernel, for the persistent grid
+  const size_t smem = mark_smem(e);
+  CU(cudaFuncSetAttribute(k_mark<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mark<MARK_BLOCK>, MARK_BLOCK, smem));
+  e->mark_occupancy = std::max(occ, 1);
+  return ES_OK;
+}
+
+}  // namespace es
+
+using namespace es;
+
+namespace es {
+// Probes: copy in, one kernel, copy out. Small and synchronous.
+template <typename Launch>
+static es_status probe(es_engine *e, size_t count, size_t in_bytes, const void *in, size_t out_bytes,
+                       std::vector<std::pair<void *, size_t>> outs, Launch launch) {
+  std::lock_guard<std::mutex> lk(e->mu);
+  cudaSetDevice(e->device);
+  void *d_in = nullptr;
+  std::vector<void *> d_outs(outs.size(), nullptr);
+  (void)out_bytes;
+  CU(cudaMalloc(&d_in, std::max<size_t>(in_bytes, 8)));
+  for (size_t i = 0; i < outs.size(); ++i) CU(cudaMalloc(&d_outs[i], std::max<size_t>(outs[i].second, 8)));
+  CU(cudaMemcpy(d_in, in, in_bytes, cudaMemcpyHostToDevice));
+  CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), e->stream));
+  launch(d_in, d_outs);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(e->stream));
+  for (size_t i = 0; i < outs.size(); ++i) CU(cudaMemcpy(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost));
+  u32 st = 0;
+  CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
+  cudaFree(d_in);
+  for (void *p : d_outs) cudaFree(p);
+  (void)count;
+  if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
+  return ES_OK;
+}
+
+}  // namespace es
+
+// ============================================================================ C ABI
+
+extern "C" {
+
+const char *es_status_str(es_status s) {
+  switch (s) {
+    case ES_OK: return "ok";
+    case ES_ERR_ARG: return "invalid argument";
+    case ES_ERR_PIN: return "class table digest mismatch";
+    case ES_ERR_RANGE: return "range outside floor/ceiling";
+    case ES_ERR_FILTERS: return "bad filter file";
+    case ES_ERR_CUDA: return "CUDA error";
+    case ES_ERR_DEVICE_STATUS: return "device status error";
+    case ES_ERR_NOMEM: return "out of memory";
+    case ES_ERR_TIMEOUT: return "timeout";
+    case ES_ERR_BUSY: return "busy";
+  }
+  return "unknown status";
+}
+
+static thread_local std::string g_open_error;   // why the last es_open on this thread failed
+
+const char *es_last_error(const es_engine *e) { return e ? e->last_error.c_str() : g_open_error.c_str(); }
+
+es_status es_load_filters(const char *path, uint64_t **mods, uint64_t **ress, size_t *n) {
+  if (!path || !mods || !ress || !n) return ES_ERR_ARG;
+  FILE *fp = fopen(path, "r");
+  if (!fp) return ES_ERR_FILTERS;
+  std::vector<uint64_t> m, r;
+  char line[256];
+  while (fgets(line, sizeof line, fp)) {
+    unsigned long long a, b;
+    if (sscanf(line, "FILTER %llu %llu", &a, &b) == 2) { m.push_back(a); r.push_back(b); }
+  }
+  fclose(fp);
+  if (m.empty()) return ES_ERR_FILTERS;
+  *mods = (uint64_t *)malloc(m.size() * sizeof(uint64_t));
+  *ress = (uint64_t *)malloc(r.size() * sizeof(uint64_t));
+  if (!*mods || !*ress) { free(*mods); free(*ress); return ES_ERR_NOMEM; }
+  memcpy(*mods, m.data(), m.size() * sizeof(uint64_t));
+  memcpy(*ress, r.data(), r.size() * sizeof(uint64_t));
+  *n = m.size();
+  return ES_OK;
+}
+
+void es_free_u64(uint64_t *p) { free(p); }
+
+es_status es_open(const es_config *cfg, es_engine **out) {
+  if (!cfg || !out) return ES_ERR_ARG;
+  *out = nullptr;
+  es_engine *e = new (std::nothrow) es_engine();
+  if (!e) return ES_ERR_NOMEM;
+  e->M = cfg->wheel_M ? cfg->wheel_M : 2042040;
+  e->mmax = cfg->mmax ? cfg->mmax : 10000;
+  e->sieve_p = cfg->sieve_p;
+  e->device = cfg->device;
+  e->flags = cfg->flags;
+  if (e->M < 2 || e->M > 0xFFFFFFFFull) { delete e; return ES_ERR_ARG; }
+  const std::vector<Cover> covers = gen_covers(e->mmax);
+  const Wheel w = build_wheel(e->M, gen_wheel_covers(e->M), gen_ucerts(UCERT_RMAX, UCERT_UMAX));
+  e->classes = w.classes;
+  e->wheel_pmin = w.max_pmin;
+  for (const Cover &f : covers) e->cover_pmax = std::max(e->cover_pmax, f.pmin);
+  e->class_fnv = fnv64_classes(e->classes);
+  e->pin = class_pin(e->M);
+  if (e->pin && e->class_fnv != e->pin->fnv64) {
+    char buf[200];
+    snprintf(buf, sizeof buf, "class table digest mismatch at M=%llu -- derived fnv64 %016llx, expected %016llx",
+             e->M, e->class_fnv, e->pin->fnv64);
+    g_open_error = buf;
+    delete e;
+    return ES_ERR_PIN;
+  }
+  if (e->classes.empty()) { delete e; return ES_ERR_ARG; }
+  if (cfg->filter_mods) {
+    if (!cfg->filter_ress || cfg->n_filters == 0) { delete e; return ES_ERR_FILTERS; }
+    e->mods.assign(cfg->filter_mods, cfg->filter_mods + cfg->n_filters);
+    e->ress.assign(cfg->filter_ress, cfg->filter_ress + cfg->n_filters);
+  } else {
+    for (const Cover &f : covers)
+      if (e->M % f.mod) { e->mods.push_back(f.mod); e->ress.push_back(f.res); }
+  }
+  e->ncov = e->mods.size();
+  if (e->sieve_p)
+    for (u64 q : small_primes(e->sieve_p, e->M)) { e->mods.push_back(q); e->ress.push_back(0); }
+  e->filter_fnv = fnv64_filters(e->mods, e->ress, e->ncov);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= e->device || e->device < 0) {
+    delete e;
+    return ES_ERR_CUDA;
+  }
+  if (cudaSetDevice(e->device) != cudaSuccess) { delete e; return ES_ERR_CUDA; }
+  cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device);
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) { delete e; return ES_ERR_CUDA; }
+  for (auto &ev : e->ev) cudaEventCreate(&ev);
+  const es_status s = build_tables(e);
+  if (s != ES_OK) {
+    g_open_error = e->last_error;
+    es_close(e);
+    return s;
+  }
+  *out = e;
+  return ES_OK;
+}
+
+es_status es_close(es_engine *e) {
+  if (!e) return ES_OK;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
+  cudaFree(e->d_K0); cudaFree(e->d_tde); cudaFree(e->d_win); cudaFree(e->d_cnt);
+  cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
+  cudaFree(e->d_ctr); cudaFree(e->d_status);
+  for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return ES_OK;
+}
+
+es_status es_run_window(es_engine *e, uint64_t lo, uint64_t hi, es_counters *out, es_records *recs) {
+  if (!e || !out) return ES_ERR_ARG;
+  std::lock_guard<std::mutex> lk(e->mu);
+  cudaSetDevice(e->device);
+  es_window w{lo, hi};
+  memset(out, 0, sizeof *out);
+  if (recs) { recs->recs = nullptr; recs->n = 0; }
+  return run_windows(e, &w, 1, ES_SCHED_PERSISTENT, out, recs);
+}
+
+es_status es_run_batch(es_engine *e, const es_window *w, size_t n, int schedule, es_counters *per_window,
+                       es_records *recs) {
+  if (!e || (!w && n) || !per_window) return ES_ERR_ARG;
+  if (schedule != ES_SCHED_PLAIN && schedule != ES_SCHED_PERSISTENT) return ES_ERR_ARG;
+  std::lock_guard<std::mutex> lk(e->mu);
+  cudaSetDevice(e->device);
+  memset(per_window, 0, n * sizeof(es_counters));
+  if (recs) { recs->recs = nullptr; recs->n = 0; }
+  if (n == 0) return ES_OK;
+  return run_windows(e, w, n, schedule, per_window, recs);
+}
+
+es_status es_free_records(es_records *r) {
+  if (!r) return ES_ERR_ARG;
+  free(r->recs);
+  r->recs = nullptr;
+  r->n = 0;
+  return ES_OK;
+}
+
+static int u128_dec(char *out, unsigned long long lo, unsigned long long hi) {
+  unsigned __int128 v = ((unsigned __int128)hi << 64) | lo;
+  char buf[48];
+  int n = 0;
+  if (!v) buf[n++] = '0';
+  while (v) { buf[n++] = (char)('0' + (int)(v % 10)); v /= 10; }
+  for (int i = 0; i < n; ++i) out[i] = buf[n - 1 - i];
+  out[n] = 0;
+  return n;
+}
+
+size_t es_format_record(const es_record *r, char *buf, size_t cap) {
+  if (!r || !buf) return 0;
+  int k = 0;
+  if (r->kind == ES_REC_RUNG) {
+    char u[48];
+    u128_dec(u, r->c, r->d);
+    k = snprintf(buf, cap, "RUNG %llu %llu %llu %s\n", (unsigned long long)r->p, (unsigned long long)r->a,
+                 (unsigned long long)r->b, u);
+  } else if (r->kind == ES_REC_SOLVED) {
+    k = snprintf(buf, cap, "SOLVED %llu %llu %llu %llu %llu\n", (unsigned long long)r->p, (unsigned long long)r->a,
+                 (unsigned long long)r->b, (unsigned long long)r->c, (unsigned long long)r->d);
+  } else if (r->kind == ES_REC_SURVIVOR) {
+    k = snprintf(buf, cap, "SURVIVOR %llu\n", (unsigned long long)r->p);
+  } else {
+    return 0;
+  }
+  return (k > 0 && (size_t)k < cap) ? (size_t)k : 0;
+}
+
+size_t es_format_summary(const es_engine *e, uint64_t lo, uint64_t hi, const es_counters *c, char *buf, size_t cap) {
+  if (!e || !c || !buf) return 0;
+  const int k = snprintf(buf, cap,
+                         "SUMMARY lo=%llu hi=%llu wheelM=%llu lanes=%zu mmax=%llu ucert_rmax=%u ucert_umax=%u "
+                         "wheel_pmin=%llu classes_sha256=%s positions=%llu covered=%llu sieved=%llu mr=%llu "
+                         "composite=%llu rung=%llu direct=%llu survivors=%llu\n",
+                         (unsigned long long)lo, (unsigned long long)hi, e->M, e->classes.size(), e->mmax,
+                         UCERT_RMAX, UCERT_UMAX, e->wheel_pmin, e->pin ? e->pin->sha256 : "unpinned",
+                         (unsigned long long)c->positions, (unsigned long long)c->covered,
+                         (unsigned long long)c->sieved, (unsigned long long)c->mr, (unsigned long long)c->composite,
+                         (unsigned long long)c->rung, (unsigned long long)c->direct,
+                         (unsigned long long)c->survivors);
+  return (k > 0 && (size_t)k < cap) ? (size_t)k : 0;
+}
+
+es_status es_info(const es_engine *e, es_info_t *o) {
+  if (!e || !o) return ES_ERR_ARG;
+  memset(o, 0, sizeof *o);
+  o->wheel_M = e->M; o->lanes = e->classes.size(); o->wheel_pmin = e->wheel_pmin;
+  o->cover_pmax = e->cover_pmax; o->floor = std::max(e->wheel_pmin, e->cover_pmax);
+  o->ceiling = DIRECT_PMAX; o->class_fnv64 = e->class_fnv; o->filter_fnv64 = e->filter_fnv;
+  o->n_certified = e->ncov; o->n_filters = e->mods.size(); o->mmax = e->mmax;
+  o->pinned = e->pin != nullptr;
+  snprintf(o->classes_sha256, sizeof o->classes_sha256, "%s", e->pin ? e->pin->sha256 : "unpinned");
+  return ES_OK;
+}
+
+es_status es_classes(const es_engine *e, uint64_t *out, size_t cap) {
+  if (!e || !out) return ES_ERR_ARG;
+  for (size_t i = 0; i < e->classes.size() && i < cap; ++i) out[i] = e->classes[i];
+  return ES_OK;
+}
+
+es_status es_timing(const es_engine *e, es_timing_t *o) {
+  if (!e || !o) return ES_ERR_ARG;
+  *o = e->timing;
+  return ES_OK;
+}
+
+es_status es_is_prime_batch(es_engine *e, const uint64_t *n, size_t count, uint8_t *out) {
+  if (!e || (!n && count) || (!out && count)) return ES_ERR_ARG;
+  if (!count) return ES_OK;
+  return probe(e, count, count * 8, n, count, {{out, count}}, [&](void *in, std::vector<void *> &o) {
+    k_probe_prime<<<e->sm_count * 2, 256, 0, e->stream>>>((const u64 *)in, count, (unsigned char *)o[0]);
+  });
+}
+
+es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_record *out, uint8_t *found) {
+  if (!e || (!p && count) || (!out && count) || (!found && count)) return ES_ERR_ARG;
+  if (!count) return ES_OK;
+  return probe(e, count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
+               [&](void *in, std::vector<void *> &o) {
+                 k_probe_rung<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
+                                                                     (unsigned char *)o[1], e->d_tdp, e->d_tde,
+                                                                     e->d_status);
+               });
+}
+
+es_status es_solve_direct_batch(es_engine *e, const uint64_t *p, size_t count, es_record *out, uint8_t *found) {
+  if (!e || (!p && count) || (!out && count) || (!found && count)) return ES_ERR_ARG;
+  if (!count) return ES_OK;
+  return probe(e, count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
+               [&](void *in, std::vector<void *> &o) {
+                 k_probe_direct<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
+                                                                       (unsigned char *)o[1], e->d_tdp, e->d_tde,
+                                                                       e->d_status);
+               });
+}
+
+es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_t *pr, uint8_t *ex, uint8_t *k) {
+  if (!e || (!n && count) || (!pr && count) || (!ex && count) || (!k && count)) return ES_ERR_ARG;
+  if (!count) return ES_OK;
+  return probe(e, count, count * 8, n, 0, {{pr, count * MAXF * 8}, {ex, count * MAXF}, {k, count}},
+               [&](void *in, std::vector<void *> &o) {
+                 k_probe_factor<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (u64 *)o[0],
+                                                                       (unsigned char *)o[1], (unsigned char *)o[2],
+                                                                       e->d_tdp, e->d_tde, e->d_status);
+               });
+}
+
+es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket) {
+  (void)w; (void)n; (void)ticket;
+  return e ? fail(e, ES_ERR_ARG, "serving queue not built yet") : ES_ERR_ARG;
+}
+
+es_status es_poll(es_engine *e, uint64_t ticket, es_counters *per_window, es_records *recs, int timeout_ms) {
+  (void)ticket; (void)per_window; (void)recs; (void)timeout_ms;
+  return e ? fail(e, ES_ERR_ARG, "serving queue not built yet") : ES_ERR_ARG;
+}
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// es_kernels.cuh -- device-side layouts shared by the kernels and the host engine.
+#pragma once
+#include <cstdint>
+#include "es_arith.cuh"
+
+namespace es {
+
+typedef unsigned short u16;
+
+constexpr u16 K0_MISS = 0xFFFF;     // the filter never hits this lane
+constexpr int DMAX = 8192;          // distinct strides held in shared memory per CTA
+
+// One scan window as the device sees it. Lane l's positions are p = rho_l + M*K for
+// K = Kfirst .. Kfirst + npos - 1, with Kfirst = Q + (rho_l < lo mod M).
+struct WinDev {
+  u64 lo, hi;
+  u64 Q;          // lo / M
+  u64 item0;      // first marking item of this window in the batch's item space
+  u32 lomod;      // lo % M
+  u32 nseg;       // segments per lane
+};
+
+// A position that no filter killed: (window, lane, J) is its key in the output order.
+struct Surv {
+  u64 p;
+  u64 J;
+  u32 win, lane;
+};
+
+// Per-window device counters; covered/sieved/mr are derived on the host from
+// positions, alive-after-covers and survivors, which are sums over segments.
+struct WinCount {
+  unsigned long long positions, after_covers, surv, composite, rung, direct, unsolved, pad;
+};
+
+// Device record: the layout of es_record.
+struct RecDev {
+  u32 kind, win, lane, reserved;
+  u64 J, p, a, b, c, d;
+};
+
+struct MarkParams {
+  const u32 *rho;          // [L] lane classes
+  const u16 *K0;           // [L][ldk] first hit K mod s per (lane, filter), or K0_MISS
+  const u32 *fdesc;        // [nf] stride s (low 16 bits) | index of s among distinct strides
+  const u32 *sdist;        // [D] distinct strides
+  const WinDev *win;       // [nwin]
+  u64 *queue;              // work-queue head (persistent schedule)
+  Surv *surv;              // survivor list
+  unsigned long long *surv_count;
+  WinCount *cnt;           // [nwin]
+  u64 total_items;
+  u64 surv_cap;
+  u64 M;
+  u32 L, ldk, nf, ncov, D, nwin, seg;
+  u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
+};
+
+struct TailParams {
+  Surv *surv;
+  unsigned long long *surv_count;
+  u32 *primes;             // indices into surv
+  unsigned long long *prime_count;
+  u32 *direct;             // indices into surv, primes that no rung certified
+  unsigned long long *direct_count;
+  RecDev *recs;
+  unsigned long long *rec_count;
+  WinCount *cnt;
+  const u32 *tdp;          // odd primes < 2^16
+  const TdEntry *tde;
+  u32 *status;
+  u64 cap;                 // capacity of surv/primes/direct/recs
+};
+
+}  // namespace es

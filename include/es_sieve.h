@@ -1,0 +1,190 @@
+/* es_sieve.h -- C ABI of the GB300 engine for the Erdos-Straus verification sieve's
+ * per-window funnel: wheel filtering against the certified class table, marking of the
+ * self-certifying cover progressions (and optional stage-B' small primes), survivor
+ * compaction, deterministic 64-bit Miller-Rabin, the rung walk (stage D) and the direct
+ * search (stage E) -- all on one GPU, results identical to the reference scanner.
+ *
+ * The reference exposes this path as a command line (sieve/rung_scan3.cpp:960-1163)
+ * over an in-process seam: sweep_lane (:711-784), solve_rung3 (:578), solve_direct3
+ * (:624). Each entry point below names the piece of that surface it replaces.
+ *
+ * Conventions: plain C types, caller-owned inputs, engine-allocated record arrays that the
+ * caller frees with es_free_records. Every failure is a status code; nothing aborts.
+ * One engine owns one GPU stream; use one engine per host thread (es_submit/es_poll are
+ * the exception: they are safe to call from several threads on one engine).
+ */
+#ifndef ES_SIEVE_H
+#define ES_SIEVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference's CLI exits 1 on every refusal (sieve/rung_scan3.cpp:
+ * 1009-1015 unknown flag, :1041-1048 pin drift, :1057-1069 ceiling/floor, :1086/:1095
+ * filter file); here each refusal has its own code. */
+typedef enum {
+  ES_OK = 0,
+  ES_ERR_ARG = 1,           /* invalid argument or unsupported parameter */
+  ES_ERR_PIN = 2,           /* derived class table does not match its pinned digest */
+  ES_ERR_RANGE = 3,         /* LO <= the filter table's pmin floor, or HI > the stage-E ceiling */
+  ES_ERR_FILTERS = 4,       /* filter file unreadable or holding no FILTER line */
+  ES_ERR_CUDA = 5,          /* CUDA runtime failure: no device, launch or copy error */
+  ES_ERR_DEVICE_STATUS = 6, /* a bounded device loop gave up (see es_last_error) */
+  ES_ERR_NOMEM = 7,         /* device or host allocation failed */
+  ES_ERR_TIMEOUT = 8,       /* es_poll: the ticket did not finish within timeout_ms */
+  ES_ERR_BUSY = 9           /* es_submit: admission refused (no free slot or memory) */
+} es_status;
+
+/* Engine configuration (the flags of sieve/rung_scan3.cpp:984-1016). */
+typedef struct {
+  uint64_t wheel_M;             /* --wheel; 0 means 2042040 */
+  uint64_t mmax;                /* --mmax; 0 means 10000 (default filter set and pmin floor) */
+  uint64_t sieve_p;             /* --sieve: stage-B' primes <= sieve_p not dividing M; 0 = off */
+  uint64_t seg;                 /* --seg: accepted for command-line parity; the device picks its
+                                   own segment (results do not depend on it); 0 = default */
+  const uint64_t *filter_mods;  /* --filters: certified (mod,res) pairs in file order; NULL =
+                                   the generated default set (covers with m <= mmax, m not | M) */
+  const uint64_t *filter_ress;
+  size_t n_filters;
+  int device;                   /* CUDA device ordinal */
+  size_t mem_budget;            /* device bytes the engine may hold for work buffers; 0 = auto */
+  uint32_t flags;               /* ES_FLAG_* */
+} es_config;
+
+/* Test hook of the frozen reference sieve (cover_scan --no-rung, sieve/cover_scan.cpp:395,
+ * :431): skip stage D so that every prime goes to the direct search. */
+#define ES_FLAG_NO_RUNG 1u
+
+/* SUMMARY counters (Scan3Stats, sieve/rung_scan3.cpp:651-660). */
+typedef struct {
+  uint64_t positions, covered, sieved, mr, composite, rung, direct, survivors;
+} es_counters;
+
+/* One certificate or survivor, binary. es_format_record renders it as the reference's
+ * text line (sieve/rung_scan3.cpp:595-599, :639-641, :781). */
+enum { ES_REC_RUNG = 1, ES_REC_SOLVED = 2, ES_REC_SURVIVOR = 3 };
+typedef struct {
+  uint32_t kind;     /* ES_REC_* */
+  uint32_t window;   /* index of the window within its batch (0 for es_run_window) */
+  uint32_t lane;     /* lane index in wheel order */
+  uint32_t reserved;
+  uint64_t J;        /* position index within the lane, from the lane's first position */
+  uint64_t p;        /* the prime */
+  uint64_t a;        /* RUNG: A = (p+r)/4     SOLVED: a */
+  uint64_t b;        /* RUNG: r               SOLVED: c */
+  uint64_t c;        /* RUNG: u, low 64 bits  SOLVED: d */
+  uint64_t d;        /* RUNG: u, high 64 bits SOLVED: k */
+} es_record;
+
+/* Records of a run, sorted by (window, lane, J): per window exactly the reference's
+ * lane-major emission order (sieve/rung_scan3.cpp:1146-1151). */
+typedef struct {
+  es_record *recs;
+  size_t n;
+} es_records;
+
+typedef struct { uint64_t lo, hi; } es_window;
+
+/* Opaque engine handle. */
+typedef struct es_engine es_engine;
+
+/* What the engine derived at es_open (the stderr banner, sieve/rung_scan3.cpp:1120-1126,
+ * and the SUMMARY's fixed fields, :1153-1158). */
+typedef struct {
+  uint64_t wheel_M;
+  uint64_t lanes;
+  uint64_t wheel_pmin;      /* max pmin over covers with m | M */
+  uint64_t cover_pmax;      /* max pmin over all covers with m <= mmax */
+  uint64_t floor;           /* LO must exceed this */
+  uint64_t ceiling;         /* HI must not exceed this (DIRECT_PMAX) */
+  uint64_t class_fnv64;
+  uint64_t filter_fnv64;    /* FNV-1a over "mod,res;" of the certified filters */
+  uint64_t n_certified;     /* ncov */
+  uint64_t n_filters;       /* certified + stage-B' primes */
+  uint64_t mmax;
+  int pinned;               /* 1 if M has a pinned class-table digest */
+  char classes_sha256[72];  /* the pin, or "unpinned" */
+} es_info_t;
+
+/* Device time of the last run, per stage, from CUDA events on the engine's stream. */
+typedef struct {
+  double total_ms, mark_ms, mr_ms, rung_ms, direct_ms;
+  uint64_t marks_kernel_launches, kernel_launches;
+  uint64_t mark_items, survivors, primes;
+} es_timing_t;
+
+/* Batch schedules: per-window launches of the same kernels, or one persistent launch over
+ * a device work queue replayed from a CUDA graph. */
+enum { ES_SCHED_PLAIN = 0, ES_SCHED_PERSISTENT = 1 };
+
+/* Derive and pin the wheel, load the filters, build the device tables. Replaces the
+ * setup of sieve/rung_scan3.cpp:1029-1126 (gen_covers, gen_wheel_covers, gen_ucerts,
+ * build_wheel, the pin check, filter loading and stage-B' append). */
+es_status es_open(const es_config *cfg, es_engine **engine_out);
+es_status es_close(es_engine *engine);
+
+/* Read a filter file ("FILTER mod res ..." lines, anything else ignored) into malloc'ed
+ * arrays, as sieve/rung_scan3.cpp:1080-1097 does. Free with es_free_u64. */
+es_status es_load_filters(const char *path, uint64_t **mods, uint64_t **ress, size_t *n);
+void es_free_u64(uint64_t *p);
+
+/* Verify every prime in [lo, hi): replaces the lane loop and merge of
+ * sieve/rung_scan3.cpp:1132-1151 over sweep_lane (:711-784). Refuses floors and
+ * ceilings like :1057-1069. recs may be NULL (counters only). */
+es_status es_run_window(es_engine *engine, uint64_t lo, uint64_t hi, es_counters *out, es_records *recs);
+
+/* Many windows at once: per_window[i] gets window i's counters; records carry their
+ * window index. schedule is ES_SCHED_PLAIN or ES_SCHED_PERSISTENT. No reference
+ * counterpart: the reference runs one window per process. */
+es_status es_run_batch(es_engine *engine, const es_window *w, size_t n, int schedule,
+                       es_counters *per_window, es_records *recs);
+
+/* Serving: queue windows for verification without waiting; collect them by ticket.
+ * Admission is by free slots and device memory (ES_ERR_BUSY when full). No reference
+ * counterpart. */
+es_status es_submit(es_engine *engine, const es_window *w, size_t n, uint64_t *ticket);
+es_status es_poll(es_engine *engine, uint64_t ticket, es_counters *per_window, es_records *recs,
+                  int timeout_ms);
+
+es_status es_free_records(es_records *recs);
+
+/* One record as its text line, newline included; returns the length (0 if cap is too
+ * small). The formats of sieve/rung_scan3.cpp:595-599, :639-641 and :781. */
+size_t es_format_record(const es_record *r, char *buf, size_t cap);
+
+/* The SUMMARY line (newline included) for a window's counters, exactly as
+ * sieve/rung_scan3.cpp:1153-1161 prints it; returns the length (0 if cap is too small). */
+size_t es_format_summary(const es_engine *engine, uint64_t lo, uint64_t hi, const es_counters *c,
+                         char *buf, size_t cap);
+
+es_status es_info(const es_engine *engine, es_info_t *out);
+/* The wheel classes in lane order (build_wheel, sieve/rung_scan3.cpp:211-226). */
+es_status es_classes(const es_engine *engine, uint64_t *out, size_t cap);
+es_status es_timing(const es_engine *engine, es_timing_t *out);
+const char *es_status_str(es_status s);
+const char *es_last_error(const es_engine *engine);
+
+/* Device probes over caller arrays: the reference's per-prime functions, batched.
+ * es_is_prime_batch: sprp2 && is_prime (sieve/rung_scan3.cpp:680-689,
+ *   census/rung_scan.cpp:76-92); out[i] = 1 for a prime.
+ * es_solve_rung_batch: solve_rung3 (sieve/rung_scan3.cpp:578-603); found[i] = 1 and
+ *   out[i] filled (kind ES_REC_RUNG) when a rung certifies p[i].
+ * es_solve_direct_batch: solve_direct3 (sieve/rung_scan3.cpp:624-647).
+ * es_factor_batch: factorA_fast (sieve/rung_scan3.cpp:410-431); primes ascending,
+ *   pr and ex hold 16 slots per value, k[i] the count. */
+es_status es_is_prime_batch(es_engine *engine, const uint64_t *n, size_t count, uint8_t *out);
+es_status es_solve_rung_batch(es_engine *engine, const uint64_t *p, size_t count, es_record *out,
+                              uint8_t *found);
+es_status es_solve_direct_batch(es_engine *engine, const uint64_t *p, size_t count, es_record *out,
+                                uint8_t *found);
+es_status es_factor_batch(es_engine *engine, const uint64_t *n, size_t count, uint64_t *pr,
+                          uint8_t *ex, uint8_t *k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ES_SIEVE_H */

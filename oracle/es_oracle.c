@@ -323,6 +323,7 @@ int es_o_solve_direct(u64 p, char *out, size_t cap) {
 
 /* ------------------------------------------------------------ certificate families */
 typedef struct { u64 mod, res, pmin; uint32_t a, c, d; u64 seq; } o_cover;
+static size_t o_small_primes(u64 P, u64 M, u64 **out);
 typedef struct { u64 mod, res; uint32_t r, u; } o_ucert;
 
 static int cover_cmp(const void *x, const void *y) {
@@ -483,6 +484,31 @@ size_t es_o_wheel(u64 M, u64 *classes, size_t cap, u64 *max_pmin, u64 *fnv, u64 
   return n;
 }
 
+/* ctypes: the generated default filter set for (M, mmax) -- covers with m <= mmax and
+ * m not dividing M, in (mod, res) order (sieve/rung_scan3.cpp:1098-1102) -- followed by the
+ * stage-B' primes <= sieve_p (:1106-1108). Returns the total count; *ncov gets the
+ * certified count; *cover_pmax the largest pmin over all covers with m <= mmax. */
+size_t es_o_default_filters(u64 M, u64 mmax, u64 sieve_p, u64 *mods, u64 *ress, size_t cap, size_t *ncov,
+                            u64 *cover_pmax) {
+  o_cover *c; size_t nc = es_o_gen_covers(mmax, &c);
+  size_t n = 0; u64 pm = 0;
+  for (size_t i = 0; i < nc; ++i) {
+    if (c[i].pmin > pm) pm = c[i].pmin;
+    if (M % c[i].mod == 0) continue;
+    if (n < cap) { mods[n] = c[i].mod; ress[n] = c[i].res; }
+    ++n;
+  }
+  free(c);
+  if (ncov) *ncov = n;
+  if (cover_pmax) *cover_pmax = pm;
+  if (sieve_p) {
+    u64 *sp; size_t nsp = o_small_primes(sieve_p, M, &sp);
+    for (size_t i = 0; i < nsp; ++i) { if (n < cap) { mods[n] = sp[i]; ress[n] = 0; } ++n; }
+    free(sp);
+  }
+  return n;
+}
+
 /* ------------------------------------------------------------ the sweep */
 typedef struct { u64 positions, covered, sieved, mr, composite, rung, direct, survivors; } o_stats;
 
@@ -574,7 +600,7 @@ static void o_sweep_lane(u64 rho, u64 lo, u64 hi, u64 M, const u64 *mods, const 
 }
 
 /* small_primes (sieve/rung_scan3.cpp:664-674): primes q <= P with q not dividing M. */
-static __attribute__((unused)) size_t o_small_primes(u64 P, u64 M, u64 **out) {
+static size_t o_small_primes(u64 P, u64 M, u64 **out) {
   uint8_t *comp = calloc(P + 1, 1);
   u64 *v = xmalloc(sizeof(u64) * (P + 1));
   size_t n = 0;

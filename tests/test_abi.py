@@ -1,0 +1,115 @@
+"""The C ABI without a GPU: the library loads, exports exactly what include/es_sieve.h
+declares, formats records like the reference, and refuses to run without a device."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+import es_sieve
+from conftest import ROOT, golden, read
+
+HEADER = os.path.join(ROOT, "include", "es_sieve.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(es_sieve.LIB_PATH):
+        import sys
+        sys.path.insert(0, ROOT)
+        import __graft_entry__
+        __graft_entry__.build()
+    return es_sieve.load_library()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(es_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for n in ("es_open", "es_close", "es_run_window", "es_run_batch", "es_submit", "es_poll", "es_free_records",
+              "es_format_record", "es_format_summary", "es_is_prime_batch", "es_solve_rung_batch",
+              "es_solve_direct_batch", "es_factor_batch"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", es_sieve.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(ln.split()[-1] for ln in out.splitlines() if ln.strip())
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    for n in declared_functions():
+        getattr(lib, n)
+
+
+def test_open_without_a_device_fails_loudly(lib):
+    if os.path.exists("/dev/nvidia0") or os.path.exists("/dev/nvidiactl"):
+        pytest.skip("a GPU is present")
+    with pytest.raises(es_sieve.EsError) as ex:
+        es_sieve.Engine(wheel=120120)
+    assert ex.value.status == es_sieve.ES_ERR_CUDA
+
+
+def _rec(**kw):
+    r = {n: 0 for n in es_sieve.RECORD_DTYPE.names}
+    r.update(kw)
+    return r
+
+
+def test_record_formats(lib):
+    # RUNG with a 128-bit witness, SOLVED, SURVIVOR: the reference's line formats
+    u = 2 ** 100 + 12345
+    assert es_sieve.format_record(_rec(kind=1, p=5000000132492525161, a=1250000033123131291, b=3,
+                                       c=u & (2 ** 64 - 1), d=u >> 64)) == \
+        "RUNG 5000000132492525161 1250000033123131291 3 %d\n" % u
+    assert es_sieve.format_record(_rec(kind=1, p=5, a=2, b=3, c=0, d=0)) == "RUNG 5 2 3 0\n"
+    assert es_sieve.format_record(_rec(kind=2, p=9223372036854775837, a=1, b=2, c=3, d=4)) == \
+        "SOLVED 9223372036854775837 1 2 3 4\n"
+    assert es_sieve.format_record(_rec(kind=3, p=18446744065119614971)) == "SURVIVOR 18446744065119614971\n"
+    assert es_sieve.format_record(_rec(kind=9)) == ""
+
+
+def test_load_filters_errors(lib, tmp_path):
+    m, r, n = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint64)(), C.c_size_t()
+    assert lib.es_load_filters(b"/nonexistent/file", C.byref(m), C.byref(r), C.byref(n)) == es_sieve.ES_ERR_FILTERS
+    empty = tmp_path / "empty.txt"
+    empty.write_text("# no filters\n")
+    assert lib.es_load_filters(str(empty).encode(), C.byref(m), C.byref(r), C.byref(n)) == es_sieve.ES_ERR_FILTERS
+    path = golden("filters", "f_M2042040_mmax2000_gpu.txt").encode()
+    assert lib.es_load_filters(path, C.byref(m), C.byref(r), C.byref(n)) == 0
+    assert n.value == 3745 and m[0] == 19 and r[0] == 15
+    lib.es_free_u64(m)
+    lib.es_free_u64(r)
+
+
+def test_status_strings(lib):
+    for s in range(10):
+        assert lib.es_status_str(s)
+
+
+def test_cli_host_modes():
+    cli = es_sieve.CLI_PATH
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    import hashlib
+    want = dict(ln.split()[::-1] for ln in read("class_tables.sha256").splitlines())
+    out = subprocess.run([cli, "--dump-classes", "--wheel", "120120"], capture_output=True).stdout
+    assert hashlib.sha256(out).hexdigest() == want["class_table_120120.txt"]
+    r = subprocess.run([cli, "1000000000000", "1000200000000", "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 1 and "unknown option" in r.stderr
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 1 and "usage" in r.stderr
+
+
+def test_cli_dump_classes_2042040():
+    cli = es_sieve.CLI_PATH
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    import hashlib
+    want = dict(ln.split()[::-1] for ln in read("class_tables.sha256").splitlines())
+    out = subprocess.run([cli, "--dump-classes"], capture_output=True).stdout
+    assert hashlib.sha256(out).hexdigest() == want["class_table_2042040.txt"]
