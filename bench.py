@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 verification-sieve engine: verified integers/s on one GB300.
+
+Workload (default `batch`): the batched configuration -- 4096 windows of lengths
+floor(2^(16 + 12 U)) and log-uniform start heights over [255255, 1.8446744065e19], seeded
+splitmix64 (erdos-strauss_gb300/workloads.py), wheel 2042040, the pruned gpu filter table.
+One step = one pass of the whole funnel (marking, compaction, Miller-Rabin, rung walk, direct
+search) over every window of the batch, through es_run_batch with the persistent schedule,
+records and counters returned to the host.
+
+  value   integers of the batch / device time of the step's kernels (CUDA events on the
+          engine's stream, inputs already resident; L2 flushed before every timed step)
+  e2e     the same integers / wall time of the es_run_batch call from host buffers
+          (window list in, counters and sorted binary records out)
+  plain   the same windows through per-window launches of the same kernels
+  c3      one 2^34-integer window at height >= 1.7e19, plain launch (the "at 1e19" row)
+
+--impl reference times the reference algorithm on the host cores (the CPU oracle port, all
+threads) on a bounded sample of the same workload. Multi-GPU: one process per GPU under
+torchrun, each rank its own seeded batch (weak scaling); value = all ranks' integers / the
+slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "erdos-strauss_gb300"))
+import workloads  # noqa: E402
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
+METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--windows", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as td
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        td.init_process_group(backend="gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def allmax(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for ln in open(self.f.name):
+            t = [x.strip() for x in ln.split(",")]
+            if len(t) >= 9:
+                rows.append(t)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def integers(wins):
+    return sum(hi - lo for lo, hi in wins)
+
+
+def l2_flusher(device):
+    """A 256 MB device buffer rewritten before every timed step (larger than the 129 MB L2)."""
+    try:
+        import torch
+        buf = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda:%d" % device)
+
+        def flush(k=[0]):
+            k[0] += 1
+            buf.fill_(k[0])
+            torch.cuda.synchronize(device)
+        return flush, "flushed (256 MB write before each timed step)"
+    except Exception as ex:  # torch missing: say so rather than hide it
+        return (lambda: None), "not flushed (%s)" % type(ex).__name__
+
+
+def cpu_baseline(wins, seconds, threads=None):
+    """The reference algorithm (CPU oracle port) on the host cores over the leading windows of
+    the workload until `seconds` have elapsed. Returns (integers/s, windows done, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import es_sieve
+    mods, ress = es_sieve.load_filters(GPU_TABLE)
+    mods, ress = [int(m) for m in mods], [int(r) for r in ress]
+    cores = threads or os.cpu_count()
+    done, ints, t0 = 0, 0, time.perf_counter()
+    for lo, hi in wins:
+        oracle.scan(lo, hi, 2042040, mods, ress, len(mods), threads=cores)
+        done += 1
+        ints += hi - lo
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    return ints / el, done, cores, el
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    wins = workloads.batch_windows(args.windows)
+    cores = os.cpu_count()
+    per_step = max(1, args.cpu_seconds / 3)
+    for _ in range(args.warmup):
+        cpu_baseline(wins[:2], 0.0, cores)
+    rates, tot_ints, tot_s, idx = [], 0, 0.0, 0
+    for k in range(args.steps):
+        rate, done, _, el = cpu_baseline(wins[idx:], per_step, cores)
+        idx = (idx + done) % len(wins)
+        rates.append(rate)
+        tot_ints += rate * el
+        tot_s += el
+    value = tot_ints / tot_s
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "integers/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "batch4096", "windows": args.windows, "wheel": 2042040,
+                       "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED},
+            "cpu_baseline": {"value": value, "unit": "integers/s", "cores": cores, "kind": "port",
+                             "sample": "each step: consecutive windows of the 4096-window batch for ~%.0f s"
+                                       % per_step},
+            "e2e": {"value": value, "unit": "integers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args, ws, rank, local):
+    import es_sieve
+    flush, flush_note = l2_flusher(local)
+    mods, ress = es_sieve.load_filters(GPU_TABLE)
+    eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local)
+    wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
+    n_int = integers(wins)
+    for _ in range(args.warmup):
+        eng.run_batch(wins)
+    barrier(ws)
+    dev_ms, wall_s, launches, recs_n, mark_ms = 0.0, 0.0, 0, 0, 0.0
+    stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush()
+            t0 = time.perf_counter()
+            per, recs = eng.run_batch(wins)
+            wall_s += time.perf_counter() - t0
+            t = eng.timing()
+            dev_ms += t["total_ms"]
+            launches += int(t["kernel_launches"])
+            recs_n = len(recs)
+            for k in stage:
+                stage[k] += t[k]
+    barrier(ws)
+    clocks = clk.summary()
+    dev_s = allmax(ws, dev_ms / 1000.0)
+    wall = allmax(ws, wall_s)
+    total_int = allsum(ws, n_int * args.steps)
+    value = total_int / dev_s
+    e2e = total_int / wall
+    extra = {}
+    if not args.no_plain:
+        flush()
+        per_p, _ = eng.run_batch(wins, schedule=es_sieve.ES_SCHED_PLAIN)
+        tp = eng.timing()
+        extra["plain"] = {"value": n_int / (tp["total_ms"] / 1000.0), "ms_per_step": tp["total_ms"],
+                          "kernel_launches": int(tp["kernel_launches"])}
+        per_b, _ = eng.run_batch(wins)
+        extra["plain"]["records_identical"] = per_p == per_b
+        c3 = workloads.c3()
+        eng.run_window(c3["lo"], c3["hi"])
+        flush()
+        eng.run_window(c3["lo"], c3["hi"])
+        t3 = eng.timing()
+        extra["c3"] = {"value": (c3["hi"] - c3["lo"]) / (t3["total_ms"] / 1000.0), "ms_per_step": t3["total_ms"],
+                       "lo": c3["lo"], "mark_ms": t3["mark_ms"], "rung_ms": t3["rung_ms"]}
+    # roofline of the dominant kernel
+    hbm, peak_kind = peaks()
+    dom = max(stage, key=stage.get)
+    info = eng.info()
+    L, ldk = info["lanes"], (info["n_filters"] + 7) // 8 * 8
+    items = eng.timing()["mark_items"]
+    mark_bytes = items * ldk * 2           # the K0 row each (window, lane, segment) item reads
+    per_launch_ms = stage[dom] / args.steps
+    if dom == "mark_ms":
+        achieved = mark_bytes / (per_launch_ms / 1000.0) / 1e9
+        roof = {"kernel": "k_mark", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes": mark_bytes}
+    else:
+        # the survivor tail reads a few bytes per prime: report it against HBM honestly
+        achieved = (recs_n * 64) / (per_launch_ms / 1000.0) / 1e9
+        roof = {"kernel": {"rung_ms": "k_rung", "mr_ms": "k_mr", "direct_ms": "k_direct"}[dom], "bound": "hbm",
+                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                "peak_kind": peak_kind, "note": "latency-bound integer tail; HBM is not its limit"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "integers/s", "cores": cores, "kind": "port",
+               "sample": "first %d windows of the batch (%.1f s, all host threads)" % (done, el)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "integers/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                "config": {"workload": "batch4096", "windows": args.windows, "integers_per_step": n_int,
+                           "wheel": 2042040, "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED,
+                           "schedule": "persistent", "l2": flush_note, "parallelism": "replicas x%d" % ws},
+                "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 * len(wins),
+                        "d2h_bytes_per_step": 64 * len(wins) + 64 * recs_n},
+                "gpu_launches": launches, "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
+                "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()}}
+        line.update(extra)
+        print(json.dumps(line))
+    eng.close()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gpu(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

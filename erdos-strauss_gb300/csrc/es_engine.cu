@@ -543,7 +543,7 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
     CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
     if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
     CU(cudaMemcpy(hc.data(), e->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost));
-    e->timing.total_ms = ev_ms(e->ev[5], e->ev[6]);
+    e->timing.total_ms = mark_ms + mr_ms + rung_ms + direct_ms;   // kernels only, inputs resident
     e->timing.mark_ms = mark_ms; e->timing.mr_ms = mr_ms;
     e->timing.rung_ms = rung_ms; e->timing.direct_ms = direct_ms;
     e->timing.marks_kernel_launches = one_pass ? 1 : n;

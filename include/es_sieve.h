@@ -110,7 +110,8 @@ typedef struct {
   char classes_sha256[72];  /* the pin, or "unpinned" */
 } es_info_t;
 
-/* Device time of the last run, per stage, from CUDA events on the engine's stream. */
+/* Device time of the last run, per stage, from CUDA events on the engine's stream;
+ * total_ms is the sum of the stages (kernels only: no host<->device copies). */
 typedef struct {
   double total_ms, mark_ms, mr_ms, rung_ms, direct_ms;
   uint64_t marks_kernel_launches, kernel_launches;

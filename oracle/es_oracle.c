@@ -620,10 +620,18 @@ static size_t o_small_primes(u64 P, u64 M, u64 **out) {
  * certified covers followed by stage-B' primes). Returns the text, malloc'ed. */
 char *es_o_scan(u64 lo, u64 hi, u64 M, const u64 *mods, const u64 *ress, size_t nall,
                 size_t ncov, u64 seg, int emit_surv, int threads, u64 *counters8) {
-  o_cover *wc; size_t nwc = es_o_gen_wheel_covers(M, &wc);
-  o_ucert *uc; size_t nuc = es_o_gen_ucerts(UCERT_RMAX, UCERT_UMAX, &uc);
-  o_wheel w = o_build_wheel(M, wc, nwc, uc, nuc);
-  free(wc); free(uc);
+  /* The wheel depends only on M: derive it once per M and keep it (the reference's
+   * driver derives it once per process, sieve/rung_scan3.cpp:1032-1034). */
+  static u64 cached_M = 0;
+  static o_wheel w;
+  if (cached_M != M) {
+    if (cached_M) free(w.classes);
+    o_cover *wc; size_t nwc = es_o_gen_wheel_covers(M, &wc);
+    o_ucert *uc; size_t nuc = es_o_gen_ucerts(UCERT_RMAX, UCERT_UMAX, &uc);
+    w = o_build_wheel(M, wc, nwc, uc, nuc);
+    free(wc); free(uc);
+    cached_M = M;
+  }
   td_init();                       /* once, before the lanes run in parallel */
   o_stats *lst = calloc(w.n, sizeof(o_stats));
   o_text *lem = calloc(w.n, sizeof(o_text));
@@ -655,7 +663,7 @@ char *es_o_scan(u64 lo, u64 hi, u64 M, const u64 *mods, const u64 *ress, size_t 
       free(lem[i].s);
     }
   }
-  free(lst); free(lem); free(w.classes);
+  free(lst); free(lem);
   const u64 c[8] = {st.positions, st.covered, st.sieved, st.mr, st.composite, st.rung, st.direct, st.survivors};
   if (counters8) memcpy(counters8, c, sizeof c);
   return out.s;
