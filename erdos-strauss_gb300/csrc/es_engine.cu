@@ -22,6 +22,7 @@
 #include "../../include/es_sieve.h"
 #include "es_arith.cuh"
 #include "es_kernels.cuh"
+#include "es_tail.cuh"
 #include "es_wheel.h"
 
 #include <cuda_runtime.h>
@@ -217,15 +218,22 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
   }
 }
 
+// Miller-Rabin, one warp per survivor, one base per lane (sprp2 && is_prime is the
+// 12-base verdict: a prime passes base 2 as well).
 __global__ void k_mr(const TailParams T) {
+  const u32 lane = threadIdx.x & 31;
+  const u64 warps = (u64)gridDim.x * blockDim.x / 32;
   const u64 n = min((u64)*T.surv_count, T.cap);
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+  for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < n; i += warps) {
     const Surv s = T.surv[i];
-    if (sprp2_64(s.p) && is_prime64(s.p)) {
-      const unsigned long long k = atomicAdd(T.prime_count, 1ull);
-      if (k < T.cap) T.primes[k] = (u32)i;
-    } else {
-      atomicAdd(&T.cnt[s.win].composite, 1ull);
+    const bool prime = warp_is_prime(s.p, lane);
+    if (lane == 0) {
+      if (prime) {
+        const unsigned long long k = atomicAdd(T.prime_count, 1ull);
+        if (k < T.cap) T.primes[k] = (u32)i;
+      } else {
+        atomicAdd(&T.cnt[s.win].composite, 1ull);
+      }
     }
   }
 }
@@ -235,20 +243,33 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
   if (k < T.cap) T.recs[k] = r;
 }
 
-__global__ void k_rung(const TailParams T, int no_rung) {
+constexpr int RUNG_WARPS = 4;
+
+// Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung).
+__global__ void __launch_bounds__(RUNG_WARPS * 32) k_rung(const TailParams T, int no_rung) {
+  __shared__ WarpFac F[RUNG_WARPS];
+  __shared__ DPWarp D[RUNG_WARPS];
+  __shared__ u64 rho_slot[RUNG_WARPS];
+  __shared__ int best_k;
+  __shared__ RungResult slot[RUNG_WARPS];
+  __shared__ RungResult res;
   const u64 n = min((u64)*T.prime_count, T.cap);
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+  for (u64 i = blockIdx.x; i < n; i += gridDim.x) {
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
-    u64 A; u32 r; U128 u;
-    if (!no_rung && solve_rung(s.p, A, r, u, T.tdp, T.tde, T.status)) {
-      RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, A, r, u.lo, u.hi};
-      put_record(T, rec);
-      atomicAdd(&T.cnt[s.win].rung, 1ull);
-    } else {
-      const unsigned long long k = atomicAdd(T.direct_count, 1ull);
-      if (k < T.cap) T.direct[k] = si;
+    const bool ok = !no_rung &&
+                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res);
+    if (threadIdx.x == 0) {
+      if (ok) {
+        RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, res.A, res.r, res.u.lo, res.u.hi};
+        put_record(T, rec);
+        atomicAdd(&T.cnt[s.win].rung, 1ull);
+      } else {
+        const unsigned long long k = atomicAdd(T.direct_count, 1ull);
+        if (k < T.cap) T.direct[k] = si;
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -271,16 +292,30 @@ __global__ void k_direct(const TailParams T) {
 
 // ---------------------------------------------------------------- probe kernels
 __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x)
-    out[i] = (sprp2_64(n[i]) && is_prime64(n[i])) ? 1 : 0;
+  const u32 lane = threadIdx.x & 31;
+  const u64 warps = (u64)gridDim.x * blockDim.x / 32;
+  for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < count; i += warps) {
+    const bool pr = warp_is_prime(n[i], lane);
+    if (lane == 0) out[i] = pr ? 1 : 0;
+  }
 }
-__global__ void k_probe_rung(const u64 *p, u64 count, RecDev *out, unsigned char *found,
-                             const u32 *tdp, const TdEntry *tde, u32 *status) {
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
-    u64 A; u32 r; U128 u;
-    const bool ok = solve_rung(p[i], A, r, u, tdp, tde, status);
-    found[i] = ok;
-    out[i] = ok ? RecDev{ES_REC_RUNG, 0, 0, 0, 0, p[i], A, r, u.lo, u.hi} : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
+__global__ void __launch_bounds__(RUNG_WARPS * 32) k_probe_rung(const u64 *p, u64 count, RecDev *out,
+                                                               unsigned char *found, const u32 *tdp,
+                                                               const TdEntry *tde, u32 *status) {
+  __shared__ WarpFac F[RUNG_WARPS];
+  __shared__ DPWarp D[RUNG_WARPS];
+  __shared__ u64 rho_slot[RUNG_WARPS];
+  __shared__ int best_k;
+  __shared__ RungResult slot[RUNG_WARPS];
+  __shared__ RungResult res;
+  for (u64 i = blockIdx.x; i < count; i += gridDim.x) {
+    const bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res);
+    if (threadIdx.x == 0) {
+      found[i] = ok;
+      out[i] = ok ? RecDev{ES_REC_RUNG, 0, 0, 0, 0, p[i], res.A, res.r, res.u.lo, res.u.hi}
+                  : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
+    }
+    __syncthreads();
   }
 }
 __global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned char *found,
@@ -292,21 +327,30 @@ __global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned ch
     out[i] = ok ? RecDev{ES_REC_SOLVED, 0, 0, 0, 0, p[i], a, c, d, k} : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
   }
 }
+// The production factorization (warp_factor), one warp per value; primes sorted ascending.
 __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *ex, unsigned char *k,
                                const u32 *tdp, const TdEntry *tde, u32 *status) {
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
-    Fac f;
-    if (!factor64(n[i], f, tdp, tde, status)) f.k = 0;
-    for (int a = 1; a < f.k; ++a)                       // ascending primes
-      for (int b = a; b > 0 && f.pr[b - 1] > f.pr[b]; --b) {
-        const u64 t = f.pr[b]; f.pr[b] = f.pr[b - 1]; f.pr[b - 1] = t;
-        const unsigned char e = f.ex[b]; f.ex[b] = f.ex[b - 1]; f.ex[b - 1] = e;
+  __shared__ WarpFac F[4];
+  __shared__ u64 rho_slot[4];
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const u64 warps = (u64)gridDim.x * blockDim.x / 32;
+  for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < count; i += warps) {
+    WarpFac &f = F[w];
+    const bool ok = warp_factor(n[i], f, tdp, tde, status, lane, rho_slot + w);
+    if (lane == 0) {
+      const int kk = ok ? f.k : 0;
+      for (int a = 1; a < kk; ++a)
+        for (int b = a; b > 0 && f.pr[b - 1] > f.pr[b]; --b) {
+          const u64 t = f.pr[b]; f.pr[b] = f.pr[b - 1]; f.pr[b - 1] = t;
+          const u32 e = f.ex[b]; f.ex[b] = f.ex[b - 1]; f.ex[b - 1] = e;
+        }
+      for (int a = 0; a < MAXF; ++a) {
+        pr[i * MAXF + a] = a < kk ? f.pr[a] : 0;
+        ex[i * MAXF + a] = a < kk ? (unsigned char)f.ex[a] : 0;
       }
-    for (int a = 0; a < MAXF; ++a) {
-      pr[i * MAXF + a] = a < f.k ? f.pr[a] : 0;
-      ex[i * MAXF + a] = a < f.k ? f.ex[a] : 0;
+      k[i] = (unsigned char)kk;
     }
-    k[i] = (unsigned char)f.k;
+    __syncwarp();
   }
 }
 
@@ -455,7 +499,7 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool per
   k_mr<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
   CU(cudaGetLastError());
   CU(cudaEventRecord(e->ev[2], e->stream));
-  k_rung<<<e->sm_count * 4, 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
+  k_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
   CU(cudaGetLastError());
   CU(cudaEventRecord(e->ev[3], e->stream));
   k_direct<<<e->sm_count, 32, 0, e->stream>>>(T);
@@ -936,7 +980,7 @@ es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_
   if (!count) return ES_OK;
   return probe(e, count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
                [&](void *in, std::vector<void *> &o) {
-                 k_probe_rung<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
+                 k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
                                                                      (unsigned char *)o[1], e->d_tdp, e->d_tde,
                                                                      e->d_status);
                });
@@ -958,7 +1002,7 @@ es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_
   if (!count) return ES_OK;
   return probe(e, count, count * 8, n, 0, {{pr, count * MAXF * 8}, {ex, count * MAXF}, {k, count}},
                [&](void *in, std::vector<void *> &o) {
-                 k_probe_factor<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (u64 *)o[0],
+                 k_probe_factor<<<e->sm_count * 4, 128, 0, e->stream>>>((const u64 *)in, count, (u64 *)o[0],
                                                                        (unsigned char *)o[1], (unsigned char *)o[2],
                                                                        e->d_tdp, e->d_tde, e->d_status);
                });

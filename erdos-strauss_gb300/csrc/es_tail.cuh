@@ -1,0 +1,313 @@
+// es_tail.cuh -- warp-cooperative survivor tail: Miller-Rabin, factorization, the rung DP.
+//
+// One prime's rung walk is a chain of dependent steps (trial division, a primality test,
+// sometimes Brent's rho, then a divisor DP), so a thread per prime is latency-bound: the
+// slowest prime sets the time of the whole window. Here every step is spread over a warp:
+//   trial division   lane i tests the odd primes i, i+32, ... below 2^16 against n by
+//                    multiplicative inverse; hits are gathered by ballot and divided out of
+//                    the cofactor with one warp-wide product of inverses per chunk
+//   primality        lanes 0..11 each run one of the 12 strong-probable-prime rounds
+//   Brent's rho      all 32 lanes walk with different constants c; the first split wins
+//                    (the factorization is unique, so which lane wins cannot change it)
+//   rung DP          lanes own residue classes t mod r and gather
+//                    nxt[t] = min_j cur[t * pr^-j] * pr^j over j <= e with the bound <= q
+// and a block of four warps walks successive rungs of one prime concurrently, keeping the
+// smallest rung that certifies (the reference's emission rule, sieve/rung_scan3.cpp:574-603).
+#pragma once
+#include "es_arith.cuh"
+
+namespace es {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+constexpr int TD_CHUNKS = (NTD + 31) / 32;     // 205 chunks of 32 primes
+constexpr u64 WARP_RHO_STEPS = 1ull << 24;     // per lane, per split
+
+struct WarpFac {          // shared memory, one per warp
+  u64 pr[MAXF];
+  u32 ex[MAXF];
+  int k;
+  int overflow;
+};
+
+// Append prime p with exponent e (merging a repeat). Lane 0 writes; all lanes call.
+__device__ __forceinline__ void wf_add(WarpFac &F, u64 p, int e, u32 lane) {
+  if (lane == 0) {
+    int i = 0;
+    for (; i < F.k; ++i) if (F.pr[i] == p) { F.ex[i] += e; break; }
+    if (i == F.k) {
+      if (F.k < MAXF) { F.pr[F.k] = p; F.ex[F.k] = e; ++F.k; } else F.overflow = 1;
+    }
+  }
+  __syncwarp();
+}
+
+// The 12-base deterministic test (census/rung_scan.cpp:76-92) with one base per lane.
+// All lanes must call; returns the same verdict in every lane.
+__device__ bool warp_is_prime(u64 n, u32 lane) {
+  bool ok = true;
+  if (n < 2) return false;
+  if (n <= 37) {
+    bool isb = false;
+    #pragma unroll
+    for (int i = 0; i < 12; ++i) isb |= (n == MR_BASES[i]);
+    return isb;
+  }
+  if (lane < 12) {
+    const u64 b = MR_BASES[lane];
+    if (n % b == 0) ok = false;
+    else {
+      const Mont M = mont_init(n);
+      u64 d = n - 1;
+      const int s = __ffsll((long long)d) - 1;
+      d >>= s;
+      ok = sprp_mont(to_mont(b, M), d, s, M);
+    }
+  }
+  return __all_sync(FULL, ok);
+}
+
+// Brent's rho in every lane with its own constant; returns a nontrivial factor of the odd
+// composite n (the same value in every lane), or 0 when every lane exhausted its budget.
+__device__ u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
+  if (lane == 0) *found = 0;
+  __syncwarp();
+  const Mont M = mont_init(n);
+  u64 result = 0;
+  u64 budget = WARP_RHO_STEPS;
+  for (u64 c = 1 + lane; c < 4096 && result == 0 && *found == 0 && budget; c += 32) {
+    const u64 cm = to_mont(c, M);
+    u64 y = to_mont(2, M), g = 1, r = 1, q = M.one, x = 0, ys = 0;
+    const u64 m = 128;
+    while (g == 1 && *found == 0) {
+      x = y;
+      if (budget < r) { budget = 0; break; }
+      budget -= r;
+      for (u64 i = 0; i < r; ++i) y = addmod(mmul(y, y, M), cm, n);
+      for (u64 k = 0; k < r && g == 1; k += m) {
+        ys = y;
+        const u64 lim = m < r - k ? m : r - k;
+        if (budget < lim) { budget = 0; break; }
+        budget -= lim;
+        for (u64 i = 0; i < lim; ++i) {
+          y = addmod(mmul(y, y, M), cm, n);
+          if (y == x) { g = n; break; }
+          q = mmul(q, x > y ? x - y : y - x, M);
+        }
+        if (g == n) break;
+        g = gcd64(q, n);
+        if (*found) break;
+      }
+      r <<= 1;
+      if (r > (1ull << 26) || budget == 0) break;
+    }
+    if (g == n || (g == 1 && budget && *found == 0)) {
+      g = 1;
+      for (u64 guard = 0; g == 1 && guard < (1ull << 20); ++guard) {
+        ys = addmod(mmul(ys, ys, M), cm, n);
+        const u64 diff = x > ys ? x - ys : ys - x;
+        g = gcd64(diff ? diff : n, n);
+        if (ys == x) break;
+      }
+    }
+    if (g != 1 && g != n) { result = g; *found = g; }
+  }
+  __syncwarp();
+  const unsigned has = __ballot_sync(FULL, result != 0);
+  if (has) return __shfl_sync(FULL, result, __ffs(has) - 1);
+  const u64 f = *found;
+  if (!f) atomicOr(status, ST_RHO_BUDGET);
+  return f;
+}
+
+// Complete factorization of n >= 1 into F (prime order as found). All lanes call.
+// Returns false when a bound was hit (status says which).
+__device__ bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
+                            u32 *status, u32 lane, volatile u64 *rho_slot) {
+  if (lane == 0) { F.k = 0; F.overflow = 0; }
+  __syncwarp();
+  if (n <= 1) return true;
+  const int tz = __ffsll((long long)n) - 1;
+  if (tz) { n >>= tz; wf_add(F, 2, tz, lane); }
+  u64 cur = n;                 // n with every prime found so far divided out
+  bool complete = true;        // every odd prime < 2^16 was tested
+  for (int c = 0; c < TD_CHUNKS; ++c) {
+    const int i = c * 32 + lane;
+    bool hit = false;
+    u64 f = 1;
+    int e = 0;
+    u32 d = 0;
+    if (i < NTD) {
+      d = __ldg(tdp + i);
+      const TdEntry t = tde[i];
+      u64 x = n * t.inv;
+      if (x <= t.lim) {
+        hit = true;
+        u64 m = x;
+        e = 1;
+        f = t.inv;
+        for (int g = 0; g < 64; ++g) {
+          x = m * t.inv;
+          if (x > t.lim) break;
+          m = x; ++e; f *= t.inv;
+        }
+      }
+    }
+    const unsigned mask = __ballot_sync(FULL, hit);
+    if (mask) {
+      const int base = F.k;
+      __syncwarp();
+      if (hit) {
+        const int pos = base + __popc(mask & ((1u << lane) - 1));
+        if (pos < MAXF) { F.pr[pos] = d; F.ex[pos] = e; }
+      }
+      u64 g = f;
+      #pragma unroll
+      for (int o = 16; o; o >>= 1) g *= __shfl_xor_sync(FULL, g, o);
+      cur *= g;                                    // exact: divides out every d^e found
+      __syncwarp();
+      if (lane == 0) {
+        const int nk = base + __popc(mask);
+        if (nk > MAXF) F.overflow = 1;
+        F.k = nk > MAXF ? MAXF : nk;
+      }
+      __syncwarp();
+    }
+    const int nx = (c + 1) * 32;
+    if (nx >= NTD) break;
+    const u64 dn = __ldg(tdp + nx);
+    if (dn * dn > cur) { complete = false; break; }   // cur is 1 or prime
+  }
+  if (cur > 1) {
+    if (!complete || cur <= 0xFFFFFFFFull) {
+      wf_add(F, cur, 1, lane);
+    } else {
+      // cur > 2^32 with no prime factor below 2^16: at most three prime factors.
+      u64 stack[4];
+      int sp = 0;
+      stack[sp++] = cur;
+      for (int guard = 0; sp > 0; ++guard) {
+        if (guard > 16) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
+        const u64 v = stack[--sp];
+        if (v == 1) continue;
+        if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
+        const u64 s = isqrt64(v);
+        if (s * s == v) { wf_add(F, s, 2, lane); continue; }
+        const u64 d = warp_rho(v, lane, rho_slot, status);
+        if (d == 0) return false;
+        if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
+        stack[sp++] = d;
+        stack[sp++] = v / d;
+      }
+    }
+  }
+  __syncwarp();
+  if (F.overflow) { if (lane == 0) atomicOr(status, ST_FAC_OVERFLOW); return false; }
+  return true;
+}
+
+// 128-bit product bound: a*b <= q for a, b < 2^128, q < 2^128 (one of a, b must be below
+// 2^64 for the product to fit at all).
+__device__ __forceinline__ bool mul_le128(U128 a, U128 b, U128 q, U128 &out) {
+  if (a.hi && b.hi) return false;
+  if (a.hi) { const U128 t = a; a = b; b = t; }     // now a < 2^64
+  bool over;
+  out = mul128_64(b, a.lo, over);
+  return !over && !lt128(q, out);
+}
+
+struct DPWarp {            // shared memory, one per warp
+  U128 cur[RCAP + 1];
+  U128 nxt[RCAP + 1];
+};
+
+// min_div_res (sieve/rung_scan3.cpp:544-565), lanes over residue classes. Returns the
+// least divisor u <= q of q^2 with u == target (mod r), or 0.
+__device__ U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, u32 target, DPWarp &D, u32 lane) {
+  const U128 INF{~0ull, ~0ull};
+  for (u32 t = lane; t < r; t += 32) D.cur[t] = (t == 1 % r) ? U128{1, 0} : INF;
+  __syncwarp();
+  for (int idx = -1; idx < F.k; ++idx) {
+    const u64 pr = idx < 0 ? p : F.pr[idx];
+    const int e = idx < 0 ? 2 : 2 * (int)F.ex[idx];
+    const u32 prm = (u32)(pr % r);
+    u32 inv = 0;                                 // prm^-1 mod r (prm is a unit: gcd(q, r) = 1)
+    for (u32 base = 0; base < r; base += 32) {
+      const u32 x = base + lane;
+      const unsigned m = __ballot_sync(FULL, x < r && (prm * x) % r == 1 % r);
+      if (m) { inv = base + __ffs(m) - 1; break; }
+    }
+    for (u32 t = lane; t < r; t += 32) {
+      U128 best = INF;
+      u32 s = t;
+      U128 pw{1, 0};
+      for (int j = 0; j <= e; ++j) {
+        if (j) {
+          bool over;
+          pw = mul128_64(pw, pr, over);
+          if (over || lt128(q, pw)) break;       // pr^j > q: nothing further fits
+          s = (s * inv) % r;
+        }
+        const U128 v = D.cur[s];
+        if (v.lo == ~0ull && v.hi == ~0ull) continue;
+        U128 cand;
+        if (mul_le128(v, pw, q, cand) && lt128(cand, best)) best = cand;
+      }
+      D.nxt[t] = best;
+    }
+    __syncwarp();
+    for (u32 t = lane; t < r; t += 32) D.cur[t] = D.nxt[t];
+    __syncwarp();
+  }
+  const U128 u = D.cur[target];
+  __syncwarp();
+  return (u.lo == ~0ull && u.hi == ~0ull) ? U128{0, 0} : u;
+}
+
+struct RungResult { u64 A; u32 r, k; U128 u; };
+
+// The rung walk of one prime by a block of W warps (solve_rung3, sieve/rung_scan3.cpp:
+// 578-603). Warp w takes rung indices k = w, w+W, ... (r = r0 + 4k) in increasing order and
+// stops once k passes the best certifying index found by any warp. Returns true in every
+// thread when some rung certifies p; the block's result is then in *out.
+template <int W>
+__device__ bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
+                                 volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out) {
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) *best_k = 0x7FFFFFFF;
+  if (lane == 0) slot[w].k = 0x7FFFFFFF;
+  __syncthreads();
+  const u32 pm4 = (u32)(p & 3);
+  const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
+  for (u32 k = w;; k += W) {
+    const u32 r = r0 + 4 * k;
+    if (r > RCAP) break;
+    // warp-uniform: every lane must take the same branch before the warp collectives below
+    if ((int)k >= __shfl_sync(FULL, *(volatile int *)best_k, 0)) break;
+    const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
+    if (!A) continue;
+    const u32 qm = (u32)(((p % r) * (A % r)) % r);
+    if (r > 1 && gcd64(qm, r) != 1) continue;
+    const u32 target = qm ? r - qm : 0;
+    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w)) break;
+    const U128 q{p * A, __umul64hi(p, A)};
+    const U128 u = warp_min_div_res(p, F[w], q, r, target, D[w], lane);
+    if (u.lo == 0 && u.hi == 0) continue;
+    if (lane == 0) {
+      slot[w] = RungResult{A, r, k, u};
+      atomicMin(best_k, (int)k);
+    }
+    break;
+  }
+  __syncthreads();
+  const int bk = *(volatile int *)best_k;
+  bool ok = false;
+  if (bk != 0x7FFFFFFF) {
+    ok = true;
+    if (threadIdx.x == 0)
+      for (int i = 0; i < W; ++i) if ((int)slot[i].k == bk) *out = slot[i];
+  }
+  __syncthreads();
+  return ok;
+}
+
+}  // namespace es
