@@ -220,7 +220,7 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.warmup):
         eng.run_batch(wins)
     barrier(ws)
-    dev_ms, wall_s, launches, recs_n, mark_ms = 0.0, 0.0, 0, 0, 0.0
+    dev_ms, wall_s, launches, recs_n, items = 0.0, 0.0, 0, 0, 0
     stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
     with Clocks(local) as clk:
         for _ in range(args.steps):
@@ -231,6 +231,7 @@ def run_gpu(args, ws, rank, local):
             t = eng.timing()
             dev_ms += t["total_ms"]
             launches += int(t["kernel_launches"])
+            items = int(t["mark_items"])
             recs_n = len(recs)
             for k in stage:
                 stage[k] += t[k]
@@ -262,7 +263,6 @@ def run_gpu(args, ws, rank, local):
     dom = max(stage, key=stage.get)
     info = eng.info()
     L, ldk = info["lanes"], (info["n_filters"] + 7) // 8 * 8
-    items = eng.timing()["mark_items"]
     mark_bytes = items * ldk * 2           # the K0 row each (window, lane, segment) item reads
     per_launch_ms = stage[dom] / args.steps
     if dom == "mark_ms":

@@ -64,10 +64,18 @@ __global__ void k_build_k0(const u32 *__restrict__ rho, u32 L, const u64 *__rest
   K0[idx] = (u16)((d / g) * (u64)invs[f] % s);
 }
 
-// Clear the progression of every filter in [from, to) over alive[0, n).
+// K0T[f][l] = K0[l][f], lanes padded to Lpad with K0_MISS.
+__global__ void k_transpose_k0(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf, u32 Lpad, u16 *__restrict__ K0T) {
+  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (u64)nf * Lpad) return;
+  const u32 f = (u32)(idx / Lpad), l = (u32)(idx % Lpad);
+  K0T[idx] = l < L ? K0[(size_t)l * ldk + f] : K0_MISS;
+}
+
+// Clear the progression of every filter in [from, to) over alive[0, n) of one lane.
 template <int BLOCK>
-__device__ __forceinline__ void mark_filters(const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
-                                             const u16 *R, unsigned char *alive, u32 from, u32 to, u32 n) {
+__device__ __forceinline__ void mark_lane(const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
+                                          const u16 *R, unsigned char *alive, u32 from, u32 to, u32 n) {
   for (u32 f = from + threadIdx.x; f < to; f += BLOCK) {
     const u32 k0 = K0row[f];
     if (k0 == K0_MISS) continue;
@@ -76,6 +84,34 @@ __device__ __forceinline__ void mark_filters(const u16 *__restrict__ K0row, cons
     int off = (int)k0 - (int)R[fd >> 16];
     if (off < 0) off += (int)s;
     for (u32 j = (u32)off; j < n; j += s) alive[j] = 0;
+  }
+}
+
+// The same for GROUP consecutive lanes at once: one 32-byte load of the transposed table
+// gives filter f's first-hit residue in all 16 lanes; lane g's bytes are
+// alive[g*SEG_SMALL, g*SEG_SMALL + n_g). R0/R1 are the segment-start residues for lanes whose
+// first position sits at K = Q and K = Q + 1 (bmask bit g set for the latter).
+template <int BLOCK>
+__device__ __forceinline__ void mark_group(const u16 *__restrict__ K0T, u32 Lpad, u32 lane_base,
+                                           const u32 *__restrict__ fdesc, const u16 *R0, const u16 *R1,
+                                           u32 bmask, const u32 (&ng)[GROUP], unsigned char *alive, u32 from,
+                                           u32 to) {
+  for (u32 f = from + threadIdx.x; f < to; f += BLOCK) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(K0T + (size_t)f * Lpad + lane_base);
+    const uint4 va = __ldg(src), vb = __ldg(src + 1);
+    const u32 w[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+    const u32 fd = __ldg(fdesc + f);
+    const int s = (int)(fd & 0xFFFFu);
+    const int r0 = R0[fd >> 16], r1 = R1[fd >> 16];
+    #pragma unroll
+    for (int g = 0; g < (int)GROUP; ++g) {
+      const int k0 = (int)((w[g >> 1] >> (16 * (g & 1))) & 0xFFFFu);
+      if (k0 == K0_MISS) continue;
+      int off = k0 - (((bmask >> g) & 1) ? r1 : r0);
+      if (off < 0) off += s;
+      unsigned char *a = alive + g * SEG_SMALL;
+      for (u32 j = (u32)off; j < ng[g]; j += (u32)s) a[j] = 0;
+    }
   }
 }
 
@@ -95,18 +131,29 @@ __device__ __forceinline__ u32 block_sum(u32 v, u32 *red) {
 }
 
 struct ItemInfo {
-  u64 first, Kb;     // first position p of the lane in the window; K of the segment start
-  u64 J0;            // position index of the segment start within the lane
-  u32 n, lane, win, valid;
+  u64 J0;                 // position index of the segment start within each lane
+  u64 first[GROUP];       // first position p of each lane in the window
+  u32 n[GROUP];           // positions of each lane in this segment (0 = inactive)
+  u32 lane_base, win, G, bmask, valid;
 };
 
+// Per-window residues (lo / M) mod s_d for every distinct stride: computed once per window
+// here, instead of once per (window, lane) item.
+__global__ void k_prep(const WinDev *__restrict__ win, u32 nwin, const u32 *__restrict__ sdist, u32 D,
+                       u16 *__restrict__ Qm) {
+  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (u64)nwin * D) return;
+  const u32 w = (u32)(idx / D), d = (u32)(idx % D);
+  Qm[idx] = (u16)(win[w].Q % sdist[d]);
+}
+
 // Items are dealt from an atomic queue (persistent schedule: gridDim = resident CTAs) or
-// one per CTA (gridDim = items). Item i of window w covers lane (i - item0) % L, segment
-// (i - item0) / L.
+// one per CTA (gridDim = items).
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persistent) {
   extern __shared__ __align__(16) unsigned char smem[];
-  u16 *R = reinterpret_cast<u16 *>(smem);
+  u16 *R0 = reinterpret_cast<u16 *>(smem);          // G = 1: R; G = GROUP: residues at K = Q
+  u16 *R1 = R0 + P.D;                                // G = GROUP: residues at K = Q + 1
   unsigned char *alive = smem + P.r_bytes;
   u32 *alive32 = reinterpret_cast<u32 *>(alive);
   __shared__ ItemInfo it;
@@ -125,52 +172,92 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
           const u32 mid = (lo + hi) >> 1;
           if (P.win[mid].item0 <= item) lo = mid; else hi = mid;
         }
-        const WinDev W = P.win[lo];
+        const WinDev &W = P.win[lo];
         const u64 rem = item - W.item0;
-        const u32 lane = (u32)(rem % P.L);
-        const u64 seg = rem / P.L;
-        const u64 rho = P.rho[lane];
-        const u64 Kfirst = W.Q + (rho < W.lomod ? 1 : 0);
-        const u64 first = rho + P.M * Kfirst;
-        if (first < W.hi) {
-          const u64 npos = (W.hi - first - 1) / P.M + 1;
-          const u64 J0 = seg * P.seg;
-          if (J0 < npos) {
-            it.first = first;
-            it.J0 = J0;
-            it.Kb = Kfirst + J0;
-            it.n = (u32)min((u64)P.seg, npos - J0);
-            it.lane = lane;
-            it.win = lo;
-            it.valid = 1;
-          }
-        }
+        it.win = lo;
+        it.G = W.G;
+        it.lane_base = W.lane0 + (u32)(rem % W.groups) * W.G;
+        it.J0 = (rem / W.groups) * W.seg;
+        it.valid = 1;
       }
     }
     __syncthreads();
     const u64 item = s_item;
     if (item >= P.total_items) break;
     next += gridDim.x;
-    if (!it.valid) { __syncthreads(); continue; }
-    const u32 n = it.n, lane = it.lane, win = it.win;
-    const u64 Kb = it.Kb;
-    // Residue of the segment's first K modulo every distinct stride.
-    for (u32 d = threadIdx.x; d < P.D; d += BLOCK) R[d] = (u16)(Kb % P.sdist[d]);
-    const u32 nw = (n + 3) >> 2;
+    const u32 win = it.win, G = it.G, lane_base = it.lane_base;
+    const u64 J0 = it.J0;
+    const WinDev &W = P.win[win];
+    if (threadIdx.x < G) {
+      const u32 lane = lane_base + threadIdx.x;
+      u32 n = 0;
+      u64 first = 0;
+      bool b = false;
+      if (lane < P.L) {
+        const u64 rho = P.rho[lane];
+        b = rho < W.lomod;
+        const u64 Kfirst = W.Q + (b ? 1 : 0);
+        first = rho + P.M * Kfirst;
+        if (first < W.hi) {
+          const u64 npos = (W.hi - first - 1) / P.M + 1;
+          if (J0 < npos) n = (u32)min((u64)W.seg, npos - J0);
+        }
+      }
+      it.n[threadIdx.x] = n;
+      it.first[threadIdx.x] = first;
+      const unsigned bm = __ballot_sync(0xFFFFFFFFu >> (32 - (G < 32 ? G : 32)), b);
+      if (threadIdx.x == 0) it.bmask = bm;
+    }
+    __syncthreads();
+    u32 ntot = 0;
+    #pragma unroll
+    for (int g = 0; g < (int)GROUP; ++g) ntot += (g < (int)G) ? it.n[g] : 0;
+    if (ntot == 0) { __syncthreads(); continue; }
+    // segment-start residues of K modulo every distinct stride
+    const u16 *Qm = P.Qm + (size_t)win * P.D;
+    if (G == 1) {
+      const u32 b = it.bmask & 1;
+      for (u32 d = threadIdx.x; d < P.D; d += BLOCK) {
+        const u32 s = P.sdist[d];
+        u32 r = (u32)Qm[d] + b + (J0 ? (u32)(J0 % s) : 0u);
+        r = r >= s ? r - s : r;
+        r = r >= s ? r - s : r;
+        R0[d] = (u16)r;
+      }
+    } else {
+      for (u32 d = threadIdx.x; d < P.D; d += BLOCK) {
+        const u32 s = P.sdist[d], q = Qm[d];
+        R0[d] = (u16)q;
+        R1[d] = (u16)(q + 1 == s ? 0 : q + 1);
+      }
+    }
+    // alive bytes: 1 for the segment's positions, 0 beyond
+    const u32 nw = G == 1 ? (it.n[0] + 3) >> 2 : GROUP * (SEG_SMALL / 4);
     for (u32 w = threadIdx.x; w < nw; w += BLOCK) {
-      const u32 left = n - 4 * w;
+      const u32 g = G == 1 ? 0 : w / (SEG_SMALL / 4);
+      const u32 jb = (G == 1 ? w : w % (SEG_SMALL / 4)) * 4;
+      const u32 n = it.n[g];
+      const u32 left = n > jb ? n - jb : 0;
       alive32[w] = left >= 4 ? 0x01010101u : (0x01010101u & ((1u << (8 * left)) - 1u));
     }
     __syncthreads();
-    const u16 *K0row = P.K0 + (size_t)lane * P.ldk;
-    mark_filters<BLOCK>(K0row, P.fdesc, R, alive, 0, P.ncov, n);      // stage B: covers
-    __syncthreads();
-    if (P.nf > P.ncov) {                                               // stage B': primes
-      u32 c = 0;
-      for (u32 w = threadIdx.x; w < nw; w += BLOCK) c += __popc(alive32[w]);
-      c = block_sum<BLOCK>(c, red);
-      if (threadIdx.x == 0) atomicAdd(&P.cnt[win].after_covers, (unsigned long long)c);
-      mark_filters<BLOCK>(K0row, P.fdesc, R, alive, P.ncov, P.nf, n);
+    u32 ng[GROUP];
+    #pragma unroll
+    for (int g = 0; g < (int)GROUP; ++g) ng[g] = (g < (int)G) ? it.n[g] : 0;
+    const u32 bmask = it.bmask;
+    for (int phase = 0; phase < 2; ++phase) {
+      const u32 from = phase ? P.ncov : 0, to = phase ? P.nf : P.ncov;
+      if (phase) {                                  // stage B': count survivors of the covers
+        if (P.nf == P.ncov) break;
+        u32 c = 0;
+        for (u32 w = threadIdx.x; w < nw; w += BLOCK) c += __popc(alive32[w]);
+        c = block_sum<BLOCK>(c, red);
+        if (threadIdx.x == 0) atomicAdd(&P.cnt[win].after_covers, (unsigned long long)c);
+      }
+      if (G == 1)
+        mark_lane<BLOCK>(P.K0 + (size_t)lane_base * P.ldk, P.fdesc, R0, alive, from, to, ng[0]);
+      else
+        mark_group<BLOCK>(P.K0T, P.Lpad, lane_base, P.fdesc, R0, R1, bmask, ng, alive, from, to);
       __syncthreads();
     }
     // Compaction: each warp takes 32 consecutive words per step; an inclusive warp scan of
@@ -194,26 +281,27 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
         if (lane_id == 0) gbase = atomicAdd(P.surv_count, (unsigned long long)tot);
         gbase = __shfl_sync(0xFFFFFFFFu, gbase, 0);
         u64 slot = gbase + incl - c;
+        const u32 g = G == 1 ? 0 : w / (SEG_SMALL / 4);
+        const u32 jb = (G == 1 ? w : w % (SEG_SMALL / 4)) * 4;
         while (x) {
           const u32 k = __ffs(x) - 1;
           x &= x - 1;
           if (slot < P.surv_cap) {
-            const u64 J = it.J0 + 4ull * w + (k >> 3);
-            Surv s;
-            s.p = it.first + P.M * J;
-            s.J = J;
-            s.win = win;
-            s.lane = lane;
-            P.surv[slot] = s;
+            const u64 J = J0 + jb + (k >> 3);
+            Surv sv;
+            sv.p = it.first[g] + P.M * J;
+            sv.J = J;
+            sv.win = win;
+            sv.lane = lane_base + g;
+            P.surv[slot] = sv;
           }
           ++slot;
         }
         mine += tot;
       }
     }
-    // `mine` is the same in every lane of a warp: lane 0 adds it once.
     if (lane_id == 0 && mine) atomicAdd(&P.cnt[win].surv, (unsigned long long)mine);
-    if (threadIdx.x == 0) atomicAdd(&P.cnt[win].positions, (unsigned long long)n);
+    if (threadIdx.x == 0) atomicAdd(&P.cnt[win].positions, (unsigned long long)ntot);
     __syncthreads();
   }
 }
@@ -357,7 +445,6 @@ __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *
 // ============================================================================ host engine
 
 constexpr int MARK_BLOCK = 128;
-constexpr u32 DEFAULT_SEG = 16384;        // positions per marking item (bytes of shared memory)
 
 struct DevBuf {
   void *p = nullptr;
@@ -377,13 +464,14 @@ struct es_engine {
   size_t ncov = 0;
   // marking order: filters sorted by stride within each phase
   std::vector<uint32_t> order;
-  uint32_t nf = 0, ldk = 0, D = 0, seg = es::DEFAULT_SEG;
+  uint32_t nf = 0, ldk = 0, D = 0, Lpad = 0;
   int device = 0, sm_count = 0, mark_occupancy = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
-  es::u16 *d_K0 = nullptr;
+  es::u16 *d_K0 = nullptr, *d_K0T = nullptr;
+  es::u16 *d_Qm = nullptr; size_t qm_cap = 0;
   es::TdEntry *d_tde = nullptr;
   // per-run buffers
   es::WinDev *d_win = nullptr; size_t win_cap = 0;
@@ -423,6 +511,13 @@ static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
     CU(cudaMalloc(&e->d_cnt, want * sizeof(WinCount)));
     e->win_cap = want;
   }
+  if ((size_t)nwin * e->D > e->qm_cap) {
+    if (e->d_Qm) cudaFree(e->d_Qm);
+    e->d_Qm = nullptr;
+    const size_t want = std::max<size_t>(nwin, 64) * std::max<u32>(e->D, 1);
+    CU(cudaMalloc(&e->d_Qm, want * sizeof(u16)));
+    e->qm_cap = want;
+  }
   if (cap > e->cap) {
     cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
     e->d_surv = nullptr; e->d_primes = e->d_direct = nullptr; e->d_recs = nullptr;
@@ -437,13 +532,14 @@ static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
 
 static MarkParams mark_params(const es_engine *e, u64 total_items, u32 nwin) {
   MarkParams P;
-  P.rho = e->d_rho; P.K0 = e->d_K0; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
+  P.rho = e->d_rho; P.K0 = e->d_K0; P.K0T = e->d_K0T; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
+  P.Qm = e->d_Qm; P.Lpad = e->Lpad;
   P.win = e->d_win; P.queue = reinterpret_cast<u64 *>(e->d_ctr + 0);
   P.surv = e->d_surv; P.surv_count = e->d_ctr + 1; P.cnt = e->d_cnt;
   P.total_items = total_items; P.surv_cap = e->cap; P.M = e->M;
   P.L = (u32)e->classes.size(); P.ldk = e->ldk; P.nf = e->nf; P.ncov = (u32)e->ncov;
-  P.D = e->D; P.nwin = nwin; P.seg = e->seg;
-  P.r_bytes = (2 * e->D + 15) & ~15u;
+  P.D = e->D; P.nwin = nwin;
+  P.r_bytes = (4 * e->D + 15) & ~15u;
   return P;
 }
 
@@ -458,23 +554,40 @@ static TailParams tail_params(const es_engine *e) {
   return T;
 }
 
-static size_t mark_smem(const es_engine *e) { return ((2 * e->D + 15) & ~15u) + e->seg + 16; }
+static size_t mark_smem(const es_engine *e) {
+  return ((4 * e->D + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
+}
 
-// Window descriptors and their item offsets (lanes x segments per window).
+// Window descriptors and their item tiling. Short windows (at most SEG_SMALL positions per
+// lane) get items of GROUP lanes over their active lane range only: when the window is
+// shorter than M, only the lanes whose class lies in [lo mod M, lo mod M + len) have a
+// position. Long windows get one lane per item and segments of SEG_BIG positions.
 static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vector<WinDev> &out) {
   out.resize(n);
   u64 items = 0;
-  const u64 L = e->classes.size();
+  const u64 L = e->classes.size(), M = e->M;
   for (size_t i = 0; i < n; ++i) {
     WinDev &d = out[i];
     d.lo = w[i].lo; d.hi = std::max(w[i].lo, w[i].hi);
-    d.Q = d.lo / e->M;
-    d.lomod = (u32)(d.lo % e->M);
+    d.Q = d.lo / M;
+    d.lomod = (u32)(d.lo % M);
     const u64 len = d.hi - d.lo;
-    const u64 maxpos = len ? (len - 1) / e->M + 1 : 0;     // most positions any lane can hold
-    d.nseg = (u32)((maxpos + e->seg - 1) / e->seg);
+    const u64 maxpos = len ? (len - 1) / M + 1 : 0;     // most positions any lane can hold
     d.item0 = items;
-    items += (u64)d.nseg * L;
+    if (maxpos <= SEG_SMALL) {
+      d.G = GROUP; d.seg = SEG_SMALL; d.nseg = maxpos ? 1 : 0;
+      u64 la = 0, lb = L;
+      if (len < M && d.lomod + len <= M) {
+        la = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod) - e->classes.begin();
+        lb = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod + len) - e->classes.begin();
+      }
+      if (la >= lb) { d.lane0 = 0; d.groups = 0; d.nseg = 0; }
+      else { d.lane0 = (u32)(la / GROUP * GROUP); d.groups = (u32)((lb - d.lane0 + GROUP - 1) / GROUP); }
+    } else {
+      d.G = 1; d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG);
+      d.lane0 = 0; d.groups = (u32)L;
+    }
+    items += (u64)d.groups * d.nseg;
   }
   return items;
 }
@@ -493,6 +606,11 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool per
                              : (unsigned)std::min<u64>(total_items, 0x7FFFFFFFull);
   if (grid == 0) grid = 1;
   CU(cudaEventRecord(e->ev[0], e->stream));
+  if (nwin && e->D) {
+    const u64 nq = (u64)nwin * e->D;
+    k_prep<<<(unsigned)((nq + 255) / 256), 256, 0, e->stream>>>(e->d_win, nwin, e->d_sdist, e->D, e->d_Qm);
+    CU(cudaGetLastError());
+  }
   k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, smem, e->stream>>>(P, persistent ? 1 : 0);
   CU(cudaGetLastError());
   CU(cudaEventRecord(e->ev[1], e->stream));
@@ -538,7 +656,7 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
   std::vector<WinDev> wd;
   const u64 total_items = describe(e, w, n, wd);
   u64 positions_bound = 0;
-  for (const WinDev &d : wd) positions_bound += (u64)d.nseg * e->seg * e->classes.size();
+  for (const WinDev &d : wd) positions_bound += (u64)d.nseg * d.seg * d.groups * d.G;
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
   cap = std::max(cap, e->cap);
   const bool one_pass = schedule == ES_SCHED_PERSISTENT || n == 1;
@@ -564,7 +682,7 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
                          cudaMemcpyHostToDevice, e->stream));
       s = launch_funnel(e, items, one_pass ? (u32)n : 1, schedule == ES_SCHED_PERSISTENT, e->d_cnt + (one_pass ? 0 : i));
       if (s) return s;
-      launches += 4;
+      launches += 5;
       CU(cudaMemcpyAsync(ctr, e->d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, e->stream));
       CU(cudaStreamSynchronize(e->stream));
       mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
@@ -685,6 +803,8 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_fdesc, std::max<size_t>(nf, 1) * sizeof(u32)));
   CU(cudaMalloc(&e->d_sdist, std::max<size_t>(sd.size(), 1) * sizeof(u32)));
   CU(cudaMalloc(&e->d_K0, (size_t)L * e->ldk * sizeof(u16)));
+  e->Lpad = (L + GROUP - 1) / GROUP * GROUP;
+  CU(cudaMalloc(&e->d_K0T, (size_t)std::max<size_t>(nf, 1) * e->Lpad * sizeof(u16)));
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
   CU(cudaMalloc(&e->d_ctr, 8 * sizeof(unsigned long long)));
@@ -706,6 +826,11 @@ static es_status build_tables(es_engine *e) {
   k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
                                                                        e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
   CU(cudaGetLastError());
+  if (nf) {
+    const u64 tt = (u64)nf * e->Lpad;
+    k_transpose_k0<<<(unsigned)((tt + 255) / 256), 256, 0, e->stream>>>(e->d_K0, L, e->ldk, (u32)nf, e->Lpad, e->d_K0T);
+    CU(cudaGetLastError());
+  }
   CU(cudaStreamSynchronize(e->stream));
   cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
   // occupancy of the marking kernel, for the persistent grid
@@ -859,7 +984,7 @@ es_status es_close(es_engine *e) {
   if (!e) return ES_OK;
   if (e->stream) cudaStreamSynchronize(e->stream);
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_tde); cudaFree(e->d_win); cudaFree(e->d_cnt);
+  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde); cudaFree(e->d_win); cudaFree(e->d_cnt);
   cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
   cudaFree(e->d_ctr); cudaFree(e->d_status);
   for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);

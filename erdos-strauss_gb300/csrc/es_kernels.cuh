@@ -11,13 +11,24 @@ constexpr u16 K0_MISS = 0xFFFF;     // the filter never hits this lane
 constexpr int DMAX = 8192;          // distinct strides held in shared memory per CTA
 
 // One scan window as the device sees it. Lane l's positions are p = rho_l + M*K for
-// K = Kfirst .. Kfirst + npos - 1, with Kfirst = Q + (rho_l < lo mod M).
+// K = Kfirst .. Kfirst + npos - 1, with Kfirst = Q + (rho_l < lo mod M). Marking items
+// are (lane group, segment) pairs: G = 1 lane per item with segments of `seg` positions
+// for long windows, or GROUP consecutive lanes per item (one segment of at most
+// SEG_SMALL positions each) for short ones, over the window's active lane range only.
+constexpr u32 GROUP = 16;
+constexpr u32 SEG_SMALL = 256;
+constexpr u32 SEG_BIG = 16384;
+
 struct WinDev {
   u64 lo, hi;
   u64 Q;          // lo / M
   u64 item0;      // first marking item of this window in the batch's item space
   u32 lomod;      // lo % M
-  u32 nseg;       // segments per lane
+  u32 G;          // lanes per item (1 or GROUP)
+  u32 seg;        // positions per segment
+  u32 nseg;       // segments
+  u32 lane0;      // first lane of the active range (a multiple of G)
+  u32 groups;     // lane groups per segment
 };
 
 // A position that no filter killed: (window, lane, J) is its key in the output order.
@@ -42,8 +53,10 @@ struct RecDev {
 struct MarkParams {
   const u32 *rho;          // [L] lane classes
   const u16 *K0;           // [L][ldk] first hit K mod s per (lane, filter), or K0_MISS
+  const u16 *K0T;          // [nf][Lpad] the same table, lane-contiguous (16-lane vector loads)
   const u32 *fdesc;        // [nf] stride s (low 16 bits) | index of s among distinct strides
   const u32 *sdist;        // [D] distinct strides
+  const u16 *Qm;           // [nwin][D] (lo / M) mod s_d per window
   const WinDev *win;       // [nwin]
   u64 *queue;              // work-queue head (persistent schedule)
   Surv *surv;              // survivor list
@@ -52,7 +65,7 @@ struct MarkParams {
   u64 total_items;
   u64 surv_cap;
   u64 M;
-  u32 L, ldk, nf, ncov, D, nwin, seg;
+  u32 L, Lpad, ldk, nf, ncov, D, nwin;
   u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
 };
 
