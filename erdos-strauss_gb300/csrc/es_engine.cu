@@ -628,7 +628,7 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool per
 
 static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0;
-  cudaEventElapsedTime(&ms, a, b);
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) { (void)cudaGetLastError(); ms = 0; }
   return ms;
 }
 
@@ -834,8 +834,12 @@ static es_status build_tables(es_engine *e) {
   CU(cudaStreamSynchronize(e->stream));
   cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
   // occupancy of the marking kernel, for the persistent grid
+  // The attribute is per function and process-wide: set it to the largest size any engine
+  // can ask for (DMAX strides), never to this engine's own size, or a second engine with
+  // fewer strides would shrink it under the first.
   const size_t smem = mark_smem(e);
-  CU(cudaFuncSetAttribute(k_mark<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem_max = ((4 * DMAX + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
+  CU(cudaFuncSetAttribute(k_mark<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
   int occ = 0;
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mark<MARK_BLOCK>, MARK_BLOCK, smem));
   e->mark_occupancy = std::max(occ, 1);
