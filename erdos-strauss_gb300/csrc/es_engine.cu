@@ -301,9 +301,146 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
       }
     }
     if (lane_id == 0 && mine) atomicAdd(&P.cnt[win].surv, (unsigned long long)mine);
-    if (threadIdx.x == 0) atomicAdd(&P.cnt[win].positions, (unsigned long long)ntot);
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------- short windows
+// OR into kill[0..nch) the residues killed by mask strides [m0, m1) and by the filters of
+// lfil[l0, l1), for a lane segment of n <= SEG_SMALL positions whose first K is congruent to
+// Qrow[d] + b modulo each stride. Lanes of the warp split the strides; the caller reduces.
+__device__ __forceinline__ void short_kill(u64 (&kill)[SEG_SMALL / 64], u32 nch, u32 n, u32 b, const u64 *tab,
+                                           const MaskDesc *__restrict__ mdesc, u32 m0, u32 m1,
+                                           const u32 *__restrict__ lfil, u32 l0, u32 l1,
+                                           const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
+                                           const u16 *__restrict__ Qrow, u32 lane) {
+  for (u32 k = m0 + lane; k < m1; k += 32) {
+    const MaskDesc md = mdesc[k];
+    u32 r = (u32)Qrow[md.d] + b;
+    if (r >= md.s) r -= md.s;
+    #pragma unroll
+    for (u32 c = 0; c < SEG_SMALL / 64; ++c) {
+      if (c < nch) {
+        const u64 *wp = tab + md.off + (r >> 6);
+        const u32 sh = r & 63;
+        kill[c] |= sh ? (wp[0] >> sh) | (wp[1] << (64 - sh)) : wp[0];
+        r += md.c64;
+        if (r >= md.s) r -= md.s;
+      }
+    }
+  }
+  for (u32 k = l0 + lane; k < l1; k += 32) {
+    const u32 f = lfil[k];
+    const u32 k0 = K0row[f];
+    if (k0 == K0_MISS) continue;
+    const u32 fd = __ldg(fdesc + f);
+    const u32 s = fd & 0xFFFFu;
+    u32 r = (u32)Qrow[fd >> 16] + b;
+    if (r >= s) r -= s;
+    int off = (int)k0 - (int)r;
+    if (off < 0) off += (int)s;
+    for (u32 j = (u32)off; j < n; j += s) {
+      #pragma unroll
+      for (u32 c = 0; c < SEG_SMALL / 64; ++c)
+        if ((j >> 6) == c) kill[c] |= 1ull << (j & 63);
+    }
+  }
+}
+
+__device__ __forceinline__ u64 warp_or(u64 v) {
+  #pragma unroll
+  for (int o = 16; o; o >>= 1) v |= __shfl_xor_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// One CTA per lane: the lane's kill-mask table is staged in shared memory with 128-bit
+// loads, then each warp takes short windows in turn and marks the lane's segment in them.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
+  extern __shared__ __align__(16) u64 tab[];
+  const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr u32 NCH = SEG_SMALL / 64;
+  for (u32 l = blockIdx.x; l < P.L; l += gridDim.x) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(P.mtab + (size_t)l * P.Wpad);
+    uint4 *dst = reinterpret_cast<uint4 *>(tab);
+    for (u32 i = threadIdx.x; i < P.Wpad / 2; i += BLOCK) dst[i] = __ldg(src + i);
+    __syncthreads();
+    const u64 rho = P.rho[l];
+    const u16 *K0row = P.K0 + (size_t)l * P.ldk;
+    for (u32 i = warp; i < P.nshort; i += BLOCK / 32) {
+      const u32 wi = P.shortw[i];
+      const WinDev W = P.win[wi];
+      const u32 b = rho < W.lomod ? 1u : 0u;
+      const u64 first = rho + P.M * (W.Q + b);
+      if (first >= W.hi) continue;
+      const u32 n = (u32)((W.hi - first - 1) / P.M + 1);
+      const u32 nch = (n + 63) >> 6;
+      const u16 *Qrow = P.Qm + (size_t)wi * P.D;
+      u64 kill[NCH] = {0, 0, 0, 0};
+      short_kill(kill, nch, n, b, tab, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow, lane);
+      u64 alive[NCH];
+      u32 cnt = 0;
+      #pragma unroll
+      for (u32 c = 0; c < NCH; ++c) {
+        const u32 lo = 64 * c;
+        const u64 valid = n >= lo + 64 ? ~0ull : (n > lo ? (1ull << (n - lo)) - 1 : 0ull);
+        alive[c] = c < nch ? valid & ~warp_or(kill[c]) : 0ull;
+        cnt += __popcll(alive[c]);
+      }
+      if (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov) {              // stage B'
+        if (lane == 0 && cnt) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
+        u64 kill2[NCH] = {0, 0, 0, 0};
+        short_kill(kill2, nch, n, b, tab, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all, K0row, P.fdesc,
+                   Qrow, lane);
+        cnt = 0;
+        #pragma unroll
+        for (u32 c = 0; c < NCH; ++c) {
+          alive[c] = c < nch ? alive[c] & ~warp_or(kill2[c]) : 0ull;
+          cnt += __popcll(alive[c]);
+        }
+      }
+      if (cnt && lane == 0) {          // survivors are rare: lane 0 writes them in order
+        u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
+        atomicAdd(&P.cnt[wi].surv, (unsigned long long)cnt);
+        #pragma unroll
+        for (u32 c = 0; c < NCH; ++c) {
+          u64 x = alive[c];
+          while (x) {
+            const u32 k = __ffsll((long long)x) - 1;
+            x &= x - 1;
+            if (slot < P.surv_cap) {
+              const u64 J = 64 * c + k;
+              Surv sv;
+              sv.p = first + P.M * J;
+              sv.J = J;
+              sv.win = wi;
+              sv.lane = l;
+              P.surv[slot] = sv;
+            }
+            ++slot;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Kill masks from the first-hit table: bit x of lane l's mask for filter f's stride, for
+// every x == K0[l][f] (mod s) below s + 64.
+__global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf, const int *__restrict__ fmask,
+                              const MaskDesc *__restrict__ mdesc, u32 Wpad, u64 *__restrict__ mtab) {
+  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (u64)L * nf) return;
+  const u32 l = (u32)(idx / nf), f = (u32)(idx % nf);
+  const int m = fmask[f];
+  if (m < 0) return;
+  const u32 k0 = K0[(size_t)l * ldk + f];
+  if (k0 == K0_MISS) return;
+  const MaskDesc md = mdesc[m];
+  u64 *row = mtab + (size_t)l * Wpad + md.off;
+  for (u32 x = k0; x < md.s + 64; x += md.s)
+    atomicOr(reinterpret_cast<unsigned long long *>(row + (x >> 6)), 1ull << (x & 63));
 }
 
 // Miller-Rabin, one warp per survivor, one base per lane (sprp2 && is_prime is the
@@ -472,6 +609,12 @@ struct es_engine {
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
   es::u16 *d_K0 = nullptr, *d_K0T = nullptr;
   es::u16 *d_Qm = nullptr; size_t qm_cap = 0;
+  // short-window kill masks
+  es::u64 *d_mtab = nullptr;
+  es::MaskDesc *d_mdesc = nullptr;
+  es::u32 *d_lfil = nullptr, *d_shortw = nullptr;
+  size_t shortw_cap = 0;
+  uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0;
   es::TdEntry *d_tde = nullptr;
   // per-run buffers
   es::WinDev *d_win = nullptr; size_t win_cap = 0;
@@ -510,6 +653,13 @@ static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
     CU(cudaMalloc(&e->d_win, want * sizeof(WinDev)));
     CU(cudaMalloc(&e->d_cnt, want * sizeof(WinCount)));
     e->win_cap = want;
+  }
+  if (nwin > e->shortw_cap) {
+    if (e->d_shortw) cudaFree(e->d_shortw);
+    e->d_shortw = nullptr;
+    const size_t want = std::max<size_t>(nwin, 64);
+    CU(cudaMalloc(&e->d_shortw, want * sizeof(u32)));
+    e->shortw_cap = want;
   }
   if ((size_t)nwin * e->D > e->qm_cap) {
     if (e->d_Qm) cudaFree(e->d_Qm);
@@ -558,12 +708,13 @@ static size_t mark_smem(const es_engine *e) {
   return ((4 * e->D + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
 }
 
-// Window descriptors and their item tiling. Short windows (at most SEG_SMALL positions per
-// lane) get items of GROUP lanes over their active lane range only: when the window is
-// shorter than M, only the lanes whose class lies in [lo mod M, lo mod M + len) have a
-// position. Long windows get one lane per item and segments of SEG_BIG positions.
-static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vector<WinDev> &out) {
+// Window descriptors and their marking items. Short windows (at most SEG_SMALL positions
+// per lane) go to k_mark_short, which walks them lane by lane; long windows get one lane per
+// item and segments of SEG_BIG positions in k_mark.
+static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vector<WinDev> &out,
+                    std::vector<u32> &shortw) {
   out.resize(n);
+  shortw.clear();
   u64 items = 0;
   const u64 L = e->classes.size(), M = e->M;
   for (size_t i = 0; i < n; ++i) {
@@ -574,28 +725,32 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
     const u64 len = d.hi - d.lo;
     const u64 maxpos = len ? (len - 1) / M + 1 : 0;     // most positions any lane can hold
     d.item0 = items;
+    d.G = 1; d.lane0 = 0;
     if (maxpos <= SEG_SMALL) {
-      d.G = GROUP; d.seg = SEG_SMALL; d.nseg = maxpos ? 1 : 0;
-      u64 la = 0, lb = L;
-      if (len < M && d.lomod + len <= M) {
-        la = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod) - e->classes.begin();
-        lb = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod + len) - e->classes.begin();
-      }
-      if (la >= lb) { d.lane0 = 0; d.groups = 0; d.nseg = 0; }
-      else { d.lane0 = (u32)(la / GROUP * GROUP); d.groups = (u32)((lb - d.lane0 + GROUP - 1) / GROUP); }
+      d.seg = SEG_SMALL; d.nseg = 0; d.groups = 0;
+      if (maxpos) shortw.push_back((u32)i);
     } else {
-      d.G = 1; d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG);
-      d.lane0 = 0; d.groups = (u32)L;
+      d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG); d.groups = (u32)L;
     }
     items += (u64)d.groups * d.nseg;
   }
   return items;
 }
 
+// Wheel positions in [lo, hi): L per full period of M, plus the classes among the residues
+// of the remainder (the sum over lanes of sieve/rung_scan3.cpp:716's npos).
+static u64 positions_in(const es_engine *e, u64 lo, u64 hi) {
+  if (hi <= lo) return 0;
+  const u64 M = e->M, len = hi - lo, a = lo % M, rem = len % M;
+  auto below = [&](u64 x) { return (u64)(std::lower_bound(e->classes.begin(), e->classes.end(), x) - e->classes.begin()); };
+  u64 part = a + rem <= M ? below(a + rem) - below(a) : (e->classes.size() - below(a)) + below(a + rem - M);
+  return (len / M) * e->classes.size() + part;
+}
+
 // One pass of the funnel over the windows described in d_win, counting into cnt.
 // `persistent` selects the queue-driven k_mark (grid = resident CTAs); otherwise one CTA
 // per item.
-static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool persistent, WinCount *cnt) {
+static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, u32 nshort, bool persistent, WinCount *cnt) {
   MarkParams P = mark_params(e, total_items, nwin);
   TailParams T = tail_params(e);
   P.cnt = cnt;
@@ -611,8 +766,20 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, bool per
     k_prep<<<(unsigned)((nq + 255) / 256), 256, 0, e->stream>>>(e->d_win, nwin, e->d_sdist, e->D, e->d_Qm);
     CU(cudaGetLastError());
   }
-  k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, smem, e->stream>>>(P, persistent ? 1 : 0);
-  CU(cudaGetLastError());
+  if (nshort) {
+    ShortParams S;
+    S.rho = e->d_rho; S.K0 = e->d_K0; S.fdesc = e->d_fdesc; S.Qm = e->d_Qm; S.mtab = e->d_mtab;
+    S.mdesc = e->d_mdesc; S.lfil = e->d_lfil; S.win = e->d_win; S.shortw = e->d_shortw;
+    S.surv = e->d_surv; S.surv_count = e->d_ctr + 1; S.cnt = cnt; S.surv_cap = e->cap; S.M = e->M;
+    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad;
+    S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all; S.nshort = nshort;
+    k_mark_short<MARK_BLOCK><<<S.L, MARK_BLOCK, (size_t)e->Wpad * 8, e->stream>>>(S);
+    CU(cudaGetLastError());
+  }
+  if (total_items) {
+    k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, smem, e->stream>>>(P, persistent ? 1 : 0);
+    CU(cudaGetLastError());
+  }
   CU(cudaEventRecord(e->ev[1], e->stream));
   k_mr<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
   CU(cudaGetLastError());
@@ -654,7 +821,8 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
       return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
   }
   std::vector<WinDev> wd;
-  const u64 total_items = describe(e, w, n, wd);
+  std::vector<u32> shortw;
+  const u64 total_items = describe(e, w, n, wd, shortw);
   u64 positions_bound = 0;
   for (const WinDev &d : wd) positions_bound += (u64)d.nseg * d.seg * d.groups * d.G;
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
@@ -677,12 +845,18 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
       // Plain schedule: the same kernels, one launch sequence per window.
       WinDev one = wd[i];
       one.item0 = 0;
-      const u64 items = one_pass ? total_items : (u64)one.nseg * e->classes.size();
+      const u64 items = one_pass ? total_items : (u64)one.nseg * one.groups;
+      const u32 zero = 0;
+      const u32 nshort = one_pass ? (u32)shortw.size() : (one.nseg == 0 && one.hi > one.lo ? 1u : 0u);
       CU(cudaMemcpyAsync(e->d_win, one_pass ? wd.data() : &one, (one_pass ? n : 1) * sizeof(WinDev),
                          cudaMemcpyHostToDevice, e->stream));
-      s = launch_funnel(e, items, one_pass ? (u32)n : 1, schedule == ES_SCHED_PERSISTENT, e->d_cnt + (one_pass ? 0 : i));
+      if (nshort)
+        CU(cudaMemcpyAsync(e->d_shortw, one_pass ? shortw.data() : &zero, nshort * sizeof(u32),
+                           cudaMemcpyHostToDevice, e->stream));
+      s = launch_funnel(e, items, one_pass ? (u32)n : 1, nshort, schedule == ES_SCHED_PERSISTENT,
+                        e->d_cnt + (one_pass ? 0 : i));
       if (s) return s;
-      launches += 5;
+      launches += 4 + (nshort ? 1 : 0) + (items ? 1 : 0);
       CU(cudaMemcpyAsync(ctr, e->d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, e->stream));
       CU(cudaStreamSynchronize(e->stream));
       mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
@@ -719,9 +893,10 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
   for (size_t i = 0; i < n; ++i) {      // the SUMMARY counters (sieve/rung_scan3.cpp:764-772)
     const WinCount &c = hc[i];
     es_counters &o = per_window[i];
-    o.positions = c.positions;
-    if (e->nf == e->ncov) { o.covered = c.positions - c.surv; o.sieved = 0; }
-    else { o.covered = c.positions - c.after_covers; o.sieved = c.after_covers - c.surv; }
+    o.positions = positions_in(e, w[i].lo, w[i].hi);
+    (void)c.positions;
+    if (e->nf == e->ncov) { o.covered = o.positions - c.surv; o.sieved = 0; }
+    else { o.covered = o.positions - c.after_covers; o.sieved = c.after_covers - c.surv; }
     o.mr = c.surv; o.composite = c.composite; o.rung = c.rung; o.direct = c.direct;
     o.survivors = c.unsolved;
   }
@@ -830,6 +1005,62 @@ static es_status build_tables(es_engine *e) {
     const u64 tt = (u64)nf * e->Lpad;
     k_transpose_k0<<<(unsigned)((tt + 255) / 256), 256, 0, e->stream>>>(e->d_K0, L, e->ldk, (u32)nf, e->Lpad, e->d_K0T);
     CU(cudaGetLastError());
+  }
+  // Kill masks for short windows: within each phase (covers, then stage-B' primes), the
+  // smallest strides get a mask while the per-lane table fits MASK_BYTES_MAX; the filters of
+  // the remaining strides are checked one by one from the first-hit table.
+  {
+    std::vector<MaskDesc> md;
+    std::vector<int> fmask(nf, -1);
+    std::vector<u32> lfil_cov, lfil_siv;
+    u32 words = 0;
+    for (int phase = 0; phase < 2; ++phase) {
+      const size_t f0 = phase ? e->ncov : 0, f1 = phase ? nf : e->ncov;
+      std::vector<u32> strides;
+      for (size_t k = f0; k < f1; ++k) strides.push_back(fdesc[k] & 0xFFFFu);
+      std::sort(strides.begin(), strides.end());
+      strides.erase(std::unique(strides.begin(), strides.end()), strides.end());
+      std::vector<int> slot_of(65536, -1);
+      for (u32 st : strides) {
+        const u32 wd = (st + 64 + 63) / 64;
+        if ((size_t)(words + wd) * 8 > MASK_BYTES_MAX) break;
+        const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
+        slot_of[st] = (int)md.size();
+        md.push_back(MaskDesc{st, di, words, 64 % st});
+        words += wd;
+      }
+      for (size_t k = f0; k < f1; ++k) {
+        const int m = slot_of[fdesc[k] & 0xFFFFu];
+        fmask[k] = m;
+        if (m < 0) (phase ? lfil_siv : lfil_cov).push_back((u32)k);
+      }
+      if (phase == 0) e->nm_cov = (u32)md.size();
+    }
+    e->nm_all = (u32)md.size();
+    e->nl_cov = (u32)lfil_cov.size();
+    e->nl_all = (u32)(lfil_cov.size() + lfil_siv.size());
+    e->Wpad = std::max<u32>(2, (words + 1) & ~1u);
+    std::vector<u32> lfil(lfil_cov);
+    lfil.insert(lfil.end(), lfil_siv.begin(), lfil_siv.end());
+    int *d_fmask = nullptr;
+    CU(cudaMalloc(&e->d_mtab, (size_t)L * e->Wpad * sizeof(u64)));
+    CU(cudaMalloc(&e->d_mdesc, std::max<size_t>(md.size(), 1) * sizeof(MaskDesc)));
+    CU(cudaMalloc(&e->d_lfil, std::max<size_t>(lfil.size(), 1) * sizeof(u32)));
+    CU(cudaMalloc(&d_fmask, std::max<size_t>(nf, 1) * sizeof(int)));
+    CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), e->stream));
+    if (!md.empty()) CU(cudaMemcpy(e->d_mdesc, md.data(), md.size() * sizeof(MaskDesc), cudaMemcpyHostToDevice));
+    if (!lfil.empty()) CU(cudaMemcpy(e->d_lfil, lfil.data(), lfil.size() * sizeof(u32), cudaMemcpyHostToDevice));
+    if (nf) CU(cudaMemcpy(d_fmask, fmask.data(), nf * sizeof(int), cudaMemcpyHostToDevice));
+    if (nf && !md.empty()) {
+      const u64 tt = (u64)L * nf;
+      k_build_masks<<<(unsigned)((tt + 255) / 256), 256, 0, e->stream>>>(e->d_K0, L, e->ldk, (u32)nf, d_fmask,
+                                                                         e->d_mdesc, e->Wpad, e->d_mtab);
+      CU(cudaGetLastError());
+    }
+    CU(cudaStreamSynchronize(e->stream));
+    cudaFree(d_fmask);
+    CU(cudaFuncSetAttribute(k_mark_short<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(MASK_BYTES_MAX + 16)));
   }
   CU(cudaStreamSynchronize(e->stream));
   cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
@@ -988,7 +1219,8 @@ es_status es_close(es_engine *e) {
   if (!e) return ES_OK;
   if (e->stream) cudaStreamSynchronize(e->stream);
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde); cudaFree(e->d_win); cudaFree(e->d_cnt);
+  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde);
+  cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil); cudaFree(e->d_shortw); cudaFree(e->d_win); cudaFree(e->d_cnt);
   cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
   cudaFree(e->d_ctr); cudaFree(e->d_status);
   for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);

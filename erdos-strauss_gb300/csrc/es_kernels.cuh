@@ -69,6 +69,31 @@ struct MarkParams {
   u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
 };
 
+// Short windows (at most SEG_SMALL positions in any lane) are marked from per-(lane, stride)
+// kill masks: for lane l and a stride s shared by several filters, bit x of the mask is set
+// when some filter of that stride kills K == x (mod s); bits [s, s + 64) repeat the pattern
+// so that any 64 consecutive residues starting below s are one funnel shift of two words.
+constexpr u32 MASK_BYTES_MAX = 48 * 1024;   // per-lane mask table budget (shared memory)
+
+struct MaskDesc { u32 s, d, off, c64; };    // stride, its index in sdist, word offset, 64 mod s
+
+struct ShortParams {
+  const u32 *rho;
+  const u16 *K0;
+  const u32 *fdesc;
+  const u16 *Qm;            // [nwin][D]
+  const u64 *mtab;          // [L][Wpad] kill masks
+  const MaskDesc *mdesc;    // covers' mask strides [0, nm_cov), then stage B' [nm_cov, nm_all)
+  const u32 *lfil;          // filters not covered by a mask: covers [0, nl_cov), then B' [nl_cov, nl_all)
+  const WinDev *win;
+  const u32 *shortw;        // indices of the short windows
+  Surv *surv;
+  unsigned long long *surv_count;
+  WinCount *cnt;
+  u64 surv_cap, M;
+  u32 L, ldk, D, Wpad, nm_cov, nm_all, nl_cov, nl_all, nshort;
+};
+
 struct TailParams {
   Surv *surv;
   unsigned long long *surv_count;
