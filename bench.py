@@ -229,6 +229,7 @@ def run_gpu(args, ws, rank, local):
             per, recs = eng.run_batch(wins)
             wall_s += time.perf_counter() - t0
             t = eng.timing()
+            last_t = t
             dev_ms += t["total_ms"]
             launches += int(t["kernel_launches"])
             items = int(t["mark_items"])
@@ -291,7 +292,8 @@ def run_gpu(args, ws, rank, local):
                 "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 * len(wins),
                         "d2h_bytes_per_step": 64 * len(wins) + 64 * recs_n},
                 "gpu_launches": launches, "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
-                "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()}}
+                "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+                "tail": {"survivors": int(last_t["survivors"]), "primes": int(last_t["primes"])}}
         line.update(extra)
         print(json.dumps(line))
     eng.close()

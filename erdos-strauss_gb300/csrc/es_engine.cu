@@ -306,26 +306,29 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 }
 
 // ---------------------------------------------------------------- short windows
-// OR into kill[0..nch) the residues killed by mask strides [m0, m1) and by the filters of
-// lfil[l0, l1), for a lane segment of n <= SEG_SMALL positions whose first K is congruent to
-// Qrow[d] + b modulo each stride. Lanes of the warp split the strides; the caller reduces.
-__device__ __forceinline__ void short_kill(u64 (&kill)[SEG_SMALL / 64], u32 nch, u32 n, u32 b, const u64 *tab,
+// kill[c] gets bit j set when position 32c + j of the lane segment (n <= SEG_SMALL positions,
+// first K congruent to Qrow[d] + b modulo each stride) is killed by a mask stride in [m0, m1)
+// or by a filter of lfil[l0, l1). Lanes of the warp split the strides; the caller reduces.
+// Mask bits come out 32 at a time: word r/32 and the next, funnel-shifted right by r mod 32.
+template <int NC>
+__device__ __forceinline__ void short_kill(u32 (&kill)[NC], u32 n, u32 b, const u32 *tab,
                                            const MaskDesc *__restrict__ mdesc, u32 m0, u32 m1,
                                            const u32 *__restrict__ lfil, u32 l0, u32 l1,
                                            const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
                                            const u16 *__restrict__ Qrow, u32 lane) {
   for (u32 k = m0 + lane; k < m1; k += 32) {
-    const MaskDesc md = mdesc[k];
-    u32 r = (u32)Qrow[md.d] + b;
-    if (r >= md.s) r -= md.s;
+    const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k);
+    const MaskDesc md{mv.x, mv.y, mv.z, mv.w};
+    const u32 s = md.s;
+    u32 r = (u32)__ldg(Qrow + md.d) + b;
+    r = r >= s ? r - s : r;
     #pragma unroll
-    for (u32 c = 0; c < SEG_SMALL / 64; ++c) {
-      if (c < nch) {
-        const u64 *wp = tab + md.off + (r >> 6);
-        const u32 sh = r & 63;
-        kill[c] |= sh ? (wp[0] >> sh) | (wp[1] << (64 - sh)) : wp[0];
-        r += md.c64;
-        if (r >= md.s) r -= md.s;
+    for (int c = 0; c < NC; ++c) {
+      const u32 *wp = tab + md.off + (r >> 5);
+      kill[c] |= __funnelshift_r(wp[0], wp[1], r & 31);
+      if (c + 1 < NC) {
+        r += md.c32;
+        r = r >= s ? r - s : r;
       }
     }
   }
@@ -335,31 +338,85 @@ __device__ __forceinline__ void short_kill(u64 (&kill)[SEG_SMALL / 64], u32 nch,
     if (k0 == K0_MISS) continue;
     const u32 fd = __ldg(fdesc + f);
     const u32 s = fd & 0xFFFFu;
-    u32 r = (u32)Qrow[fd >> 16] + b;
-    if (r >= s) r -= s;
+    u32 r = (u32)__ldg(Qrow + (fd >> 16)) + b;
+    r = r >= s ? r - s : r;
     int off = (int)k0 - (int)r;
     if (off < 0) off += (int)s;
     for (u32 j = (u32)off; j < n; j += s) {
       #pragma unroll
-      for (u32 c = 0; c < SEG_SMALL / 64; ++c)
-        if ((j >> 6) == c) kill[c] |= 1ull << (j & 63);
+      for (int c = 0; c < NC; ++c)
+        if ((j >> 5) == (u32)c) kill[c] |= 1u << (j & 31);
     }
   }
 }
 
-__device__ __forceinline__ u64 warp_or(u64 v) {
+__device__ __forceinline__ u32 warp_or32(u32 v) {
   #pragma unroll
   for (int o = 16; o; o >>= 1) v |= __shfl_xor_sync(0xFFFFFFFFu, v, o);
   return v;
+}
+
+// One lane segment of one short window, NC 32-position chunks (n <= 32 * NC).
+template <int NC>
+__device__ __forceinline__ void short_segment(const ShortParams &P, const u32 *tab, u32 l, u32 wi, u64 first,
+                                              u32 n, u32 b, const u16 *K0row, u32 lane) {
+  const u16 *Qrow = P.Qm + (size_t)wi * P.D;
+  u32 kill[NC];
+  #pragma unroll
+  for (int c = 0; c < NC; ++c) kill[c] = 0;
+  short_kill<NC>(kill, n, b, tab, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow, lane);
+  u32 alive[NC];
+  u32 cnt = 0;
+  #pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const u32 lo = 32 * c;
+    const u32 valid = n >= lo + 32 ? ~0u : (n > lo ? (1u << (n - lo)) - 1 : 0u);
+    alive[c] = valid & ~warp_or32(kill[c]);
+    cnt += __popc(alive[c]);
+  }
+  if (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov) {                  // stage B'
+    if (lane == 0 && cnt) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) kill[c] = 0;
+    short_kill<NC>(kill, n, b, tab, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all, K0row, P.fdesc, Qrow,
+                   lane);
+    cnt = 0;
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      alive[c] &= ~warp_or32(kill[c]);
+      cnt += __popc(alive[c]);
+    }
+  }
+  if (cnt && lane == 0) {              // survivors are rare: lane 0 writes them in order
+    u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
+    atomicAdd(&P.cnt[wi].surv, (unsigned long long)cnt);
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      u32 x = alive[c];
+      while (x) {
+        const u32 k = __ffs(x) - 1;
+        x &= x - 1;
+        if (slot < P.surv_cap) {
+          const u64 J = 32 * c + k;
+          Surv sv;
+          sv.p = first + P.M * J;
+          sv.J = J;
+          sv.win = wi;
+          sv.lane = l;
+          P.surv[slot] = sv;
+        }
+        ++slot;
+      }
+    }
+  }
 }
 
 // One CTA per lane: the lane's kill-mask table is staged in shared memory with 128-bit
 // loads, then each warp takes short windows in turn and marks the lane's segment in them.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
-  extern __shared__ __align__(16) u64 tab[];
+  extern __shared__ __align__(16) u32 tab[];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr u32 NCH = SEG_SMALL / 64;
   for (u32 l = blockIdx.x; l < P.L; l += gridDim.x) {
     const uint4 *src = reinterpret_cast<const uint4 *>(P.mtab + (size_t)l * P.Wpad);
     uint4 *dst = reinterpret_cast<uint4 *>(tab);
@@ -368,58 +425,21 @@ __global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
     const u64 rho = P.rho[l];
     const u16 *K0row = P.K0 + (size_t)l * P.ldk;
     for (u32 i = warp; i < P.nshort; i += BLOCK / 32) {
-      const u32 wi = P.shortw[i];
-      const WinDev W = P.win[wi];
+      const ShortWin W = P.shortw[i];
+      if (l < W.la || l >= W.lb) continue;
       const u32 b = rho < W.lomod ? 1u : 0u;
       const u64 first = rho + P.M * (W.Q + b);
       if (first >= W.hi) continue;
       const u32 n = (u32)((W.hi - first - 1) / P.M + 1);
-      const u32 nch = (n + 63) >> 6;
-      const u16 *Qrow = P.Qm + (size_t)wi * P.D;
-      u64 kill[NCH] = {0, 0, 0, 0};
-      short_kill(kill, nch, n, b, tab, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow, lane);
-      u64 alive[NCH];
-      u32 cnt = 0;
-      #pragma unroll
-      for (u32 c = 0; c < NCH; ++c) {
-        const u32 lo = 64 * c;
-        const u64 valid = n >= lo + 64 ? ~0ull : (n > lo ? (1ull << (n - lo)) - 1 : 0ull);
-        alive[c] = c < nch ? valid & ~warp_or(kill[c]) : 0ull;
-        cnt += __popcll(alive[c]);
-      }
-      if (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov) {              // stage B'
-        if (lane == 0 && cnt) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
-        u64 kill2[NCH] = {0, 0, 0, 0};
-        short_kill(kill2, nch, n, b, tab, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all, K0row, P.fdesc,
-                   Qrow, lane);
-        cnt = 0;
-        #pragma unroll
-        for (u32 c = 0; c < NCH; ++c) {
-          alive[c] = c < nch ? alive[c] & ~warp_or(kill2[c]) : 0ull;
-          cnt += __popcll(alive[c]);
-        }
-      }
-      if (cnt && lane == 0) {          // survivors are rare: lane 0 writes them in order
-        u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
-        atomicAdd(&P.cnt[wi].surv, (unsigned long long)cnt);
-        #pragma unroll
-        for (u32 c = 0; c < NCH; ++c) {
-          u64 x = alive[c];
-          while (x) {
-            const u32 k = __ffsll((long long)x) - 1;
-            x &= x - 1;
-            if (slot < P.surv_cap) {
-              const u64 J = 64 * c + k;
-              Surv sv;
-              sv.p = first + P.M * J;
-              sv.J = J;
-              sv.win = wi;
-              sv.lane = l;
-              P.surv[slot] = sv;
-            }
-            ++slot;
-          }
-        }
+      switch ((n + 31) >> 5) {
+        case 1: short_segment<1>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 2: short_segment<2>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 3: short_segment<3>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 4: short_segment<4>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 5: short_segment<5>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 6: short_segment<6>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        case 7: short_segment<7>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+        default: short_segment<8>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
       }
     }
     __syncthreads();
@@ -427,7 +447,8 @@ __global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
 }
 
 // Kill masks from the first-hit table: bit x of lane l's mask for filter f's stride, for
-// every x == K0[l][f] (mod s) below s + 64.
+// every x == K0[l][f] (mod s) below s + 32 (the repeat that a 32-bit window starting below s
+// may reach).
 __global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf, const int *__restrict__ fmask,
                               const MaskDesc *__restrict__ mdesc, u32 Wpad, u64 *__restrict__ mtab) {
   const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -438,24 +459,39 @@ __global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf
   const u32 k0 = K0[(size_t)l * ldk + f];
   if (k0 == K0_MISS) return;
   const MaskDesc md = mdesc[m];
-  u64 *row = mtab + (size_t)l * Wpad + md.off;
-  for (u32 x = k0; x < md.s + 64; x += md.s)
-    atomicOr(reinterpret_cast<unsigned long long *>(row + (x >> 6)), 1ull << (x & 63));
+  u32 *row = reinterpret_cast<u32 *>(mtab + (size_t)l * Wpad) + md.off;
+  for (u32 x = k0; x < md.s + 32; x += md.s) atomicOr(row + (x >> 5), 1u << (x & 31));
 }
 
-// Miller-Rabin, one warp per survivor, one base per lane (sprp2 && is_prime is the
-// 12-base verdict: a prime passes base 2 as well).
+// Miller-Rabin in two passes. Nearly every survivor is composite and fails the base-2
+// round (sprp2, sieve/rung_scan3.cpp:680-689), so pass one runs that round with a thread per
+// survivor; the few that pass get the 12-base test (census/rung_scan.cpp:76-92) with one base
+// per lane of a warp. A prime passes base 2, so the two passes give exactly is_prime.
 __global__ void k_mr(const TailParams T) {
+  const u64 n = min((u64)*T.surv_count, T.cap);
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const Surv s = T.surv[i];
+    if (sprp2_64(s.p)) {
+      const unsigned long long k = atomicAdd(T.cand_count, 1ull);
+      if (k < T.cap) T.cand[k] = (u32)i;
+    } else {
+      atomicAdd(&T.cnt[s.win].composite, 1ull);
+    }
+  }
+}
+
+__global__ void k_mr2(const TailParams T) {
   const u32 lane = threadIdx.x & 31;
   const u64 warps = (u64)gridDim.x * blockDim.x / 32;
-  const u64 n = min((u64)*T.surv_count, T.cap);
+  const u64 n = min((u64)*T.cand_count, T.cap);
   for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < n; i += warps) {
-    const Surv s = T.surv[i];
+    const u32 si = T.cand[i];
+    const Surv s = T.surv[si];
     const bool prime = warp_is_prime(s.p, lane);
     if (lane == 0) {
       if (prime) {
         const unsigned long long k = atomicAdd(T.prime_count, 1ull);
-        if (k < T.cap) T.primes[k] = (u32)i;
+        if (k < T.cap) T.primes[k] = si;
       } else {
         atomicAdd(&T.cnt[s.win].composite, 1ull);
       }
@@ -582,6 +618,7 @@ __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *
 // ============================================================================ host engine
 
 constexpr int MARK_BLOCK = 128;
+constexpr int SHORT_BLOCK = 256;
 
 struct DevBuf {
   void *p = nullptr;
@@ -612,7 +649,8 @@ struct es_engine {
   // short-window kill masks
   es::u64 *d_mtab = nullptr;
   es::MaskDesc *d_mdesc = nullptr;
-  es::u32 *d_lfil = nullptr, *d_shortw = nullptr;
+  es::u32 *d_lfil = nullptr;
+  es::ShortWin *d_shortw = nullptr;
   size_t shortw_cap = 0;
   uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0;
   es::TdEntry *d_tde = nullptr;
@@ -620,7 +658,7 @@ struct es_engine {
   es::WinDev *d_win = nullptr; size_t win_cap = 0;
   es::WinCount *d_cnt = nullptr;
   es::Surv *d_surv = nullptr;
-  es::u32 *d_primes = nullptr, *d_direct = nullptr;
+  es::u32 *d_primes = nullptr, *d_direct = nullptr, *d_cand = nullptr;
   es::RecDev *d_recs = nullptr;
   size_t cap = 0;
   unsigned long long *d_ctr = nullptr;   // [0] queue [1] surv [2] prime [3] direct [4] rec
@@ -658,7 +696,7 @@ static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
     if (e->d_shortw) cudaFree(e->d_shortw);
     e->d_shortw = nullptr;
     const size_t want = std::max<size_t>(nwin, 64);
-    CU(cudaMalloc(&e->d_shortw, want * sizeof(u32)));
+    CU(cudaMalloc(&e->d_shortw, want * sizeof(ShortWin)));
     e->shortw_cap = want;
   }
   if ((size_t)nwin * e->D > e->qm_cap) {
@@ -669,11 +707,12 @@ static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
     e->qm_cap = want;
   }
   if (cap > e->cap) {
-    cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
-    e->d_surv = nullptr; e->d_primes = e->d_direct = nullptr; e->d_recs = nullptr;
+    cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
+    e->d_surv = nullptr; e->d_primes = e->d_direct = e->d_cand = nullptr; e->d_recs = nullptr;
     CU(cudaMalloc(&e->d_surv, cap * sizeof(Surv)));
     CU(cudaMalloc(&e->d_primes, cap * sizeof(u32)));
     CU(cudaMalloc(&e->d_direct, cap * sizeof(u32)));
+    CU(cudaMalloc(&e->d_cand, cap * sizeof(u32)));
     CU(cudaMalloc(&e->d_recs, cap * sizeof(RecDev)));
     e->cap = cap;
   }
@@ -696,6 +735,7 @@ static MarkParams mark_params(const es_engine *e, u64 total_items, u32 nwin) {
 static TailParams tail_params(const es_engine *e) {
   TailParams T;
   T.surv = e->d_surv; T.surv_count = e->d_ctr + 1;
+  T.cand = e->d_cand; T.cand_count = e->d_ctr + 5;
   T.primes = e->d_primes; T.prime_count = e->d_ctr + 2;
   T.direct = e->d_direct; T.direct_count = e->d_ctr + 3;
   T.recs = e->d_recs; T.rec_count = e->d_ctr + 4;
@@ -712,7 +752,7 @@ static size_t mark_smem(const es_engine *e) {
 // per lane) go to k_mark_short, which walks them lane by lane; long windows get one lane per
 // item and segments of SEG_BIG positions in k_mark.
 static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vector<WinDev> &out,
-                    std::vector<u32> &shortw) {
+                    std::vector<ShortWin> &shortw) {
   out.resize(n);
   shortw.clear();
   u64 items = 0;
@@ -728,7 +768,16 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
     d.G = 1; d.lane0 = 0;
     if (maxpos <= SEG_SMALL) {
       d.seg = SEG_SMALL; d.nseg = 0; d.groups = 0;
-      if (maxpos) shortw.push_back((u32)i);
+      if (maxpos) {
+        // Shorter than M: only the classes in [lo mod M, lo mod M + len) have a position,
+        // a contiguous lane range unless it wraps past M.
+        u64 la = 0, lb = L;
+        if (len < M && d.lomod + len <= M) {
+          la = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod) - e->classes.begin();
+          lb = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod + len) - e->classes.begin();
+        }
+        if (la < lb) shortw.push_back(ShortWin{d.Q, d.hi, d.lomod, (u32)i, (u32)la, (u32)lb});
+      }
     } else {
       d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG); d.groups = (u32)L;
     }
@@ -773,7 +822,7 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, u32 nsho
     S.surv = e->d_surv; S.surv_count = e->d_ctr + 1; S.cnt = cnt; S.surv_cap = e->cap; S.M = e->M;
     S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad;
     S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all; S.nshort = nshort;
-    k_mark_short<MARK_BLOCK><<<S.L, MARK_BLOCK, (size_t)e->Wpad * 8, e->stream>>>(S);
+    k_mark_short<SHORT_BLOCK><<<S.L, SHORT_BLOCK, (size_t)e->Wpad * 8, e->stream>>>(S);
     CU(cudaGetLastError());
   }
   if (total_items) {
@@ -783,8 +832,10 @@ static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, u32 nsho
   CU(cudaEventRecord(e->ev[1], e->stream));
   k_mr<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
   CU(cudaGetLastError());
+  k_mr2<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
+  CU(cudaGetLastError());
   CU(cudaEventRecord(e->ev[2], e->stream));
-  k_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
+  k_rung<<<e->sm_count * 6, RUNG_WARPS * 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
   CU(cudaGetLastError());
   CU(cudaEventRecord(e->ev[3], e->stream));
   k_direct<<<e->sm_count, 32, 0, e->stream>>>(T);
@@ -821,7 +872,7 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
       return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
   }
   std::vector<WinDev> wd;
-  std::vector<u32> shortw;
+  std::vector<ShortWin> shortw;
   const u64 total_items = describe(e, w, n, wd, shortw);
   u64 positions_bound = 0;
   for (const WinDev &d : wd) positions_bound += (u64)d.nseg * d.seg * d.groups * d.G;
@@ -846,17 +897,24 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
       WinDev one = wd[i];
       one.item0 = 0;
       const u64 items = one_pass ? total_items : (u64)one.nseg * one.groups;
-      const u32 zero = 0;
-      const u32 nshort = one_pass ? (u32)shortw.size() : (one.nseg == 0 && one.hi > one.lo ? 1u : 0u);
+      // plain schedule: this window's short-window entry (if any), re-indexed to window 0
+      ShortWin one_short{};
+      u32 nshort = 0;
+      if (one_pass) {
+        nshort = (u32)shortw.size();
+      } else {
+        for (const ShortWin &sw : shortw)
+          if (sw.wi == i) { one_short = sw; one_short.wi = 0; nshort = 1; break; }
+      }
       CU(cudaMemcpyAsync(e->d_win, one_pass ? wd.data() : &one, (one_pass ? n : 1) * sizeof(WinDev),
                          cudaMemcpyHostToDevice, e->stream));
       if (nshort)
-        CU(cudaMemcpyAsync(e->d_shortw, one_pass ? shortw.data() : &zero, nshort * sizeof(u32),
+        CU(cudaMemcpyAsync(e->d_shortw, one_pass ? shortw.data() : &one_short, nshort * sizeof(ShortWin),
                            cudaMemcpyHostToDevice, e->stream));
       s = launch_funnel(e, items, one_pass ? (u32)n : 1, nshort, schedule == ES_SCHED_PERSISTENT,
                         e->d_cnt + (one_pass ? 0 : i));
       if (s) return s;
-      launches += 4 + (nshort ? 1 : 0) + (items ? 1 : 0);
+      launches += 5 + (nshort ? 1 : 0) + (items ? 1 : 0);
       CU(cudaMemcpyAsync(ctr, e->d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, e->stream));
       CU(cudaStreamSynchronize(e->stream));
       mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
@@ -1022,11 +1080,13 @@ static es_status build_tables(es_engine *e) {
       strides.erase(std::unique(strides.begin(), strides.end()), strides.end());
       std::vector<int> slot_of(65536, -1);
       for (u32 st : strides) {
-        const u32 wd = (st + 64 + 63) / 64;
-        if ((size_t)(words + wd) * 8 > MASK_BYTES_MAX) break;
+        // bits [0, s + 32) plus one spare word, so that the second word of a window that starts
+        // at any residue below s is inside the stride's slice
+        const u32 wd = (st + 32 + 31) / 32 + 1;
+        if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX) break;
         const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
         slot_of[st] = (int)md.size();
-        md.push_back(MaskDesc{st, di, words, 64 % st});
+        md.push_back(MaskDesc{st, di, words, 32 % st});
         words += wd;
       }
       for (size_t k = f0; k < f1; ++k) {
@@ -1039,7 +1099,7 @@ static es_status build_tables(es_engine *e) {
     e->nm_all = (u32)md.size();
     e->nl_cov = (u32)lfil_cov.size();
     e->nl_all = (u32)(lfil_cov.size() + lfil_siv.size());
-    e->Wpad = std::max<u32>(2, (words + 1) & ~1u);
+    e->Wpad = std::max<u32>(2, ((words + 1) / 2 + 1) & ~1u);   // in 64-bit words, even
     std::vector<u32> lfil(lfil_cov);
     lfil.insert(lfil.end(), lfil_siv.begin(), lfil_siv.end());
     int *d_fmask = nullptr;
@@ -1059,7 +1119,7 @@ static es_status build_tables(es_engine *e) {
     }
     CU(cudaStreamSynchronize(e->stream));
     cudaFree(d_fmask);
-    CU(cudaFuncSetAttribute(k_mark_short<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(MASK_BYTES_MAX + 16)));
   }
   CU(cudaStreamSynchronize(e->stream));
@@ -1221,7 +1281,7 @@ es_status es_close(es_engine *e) {
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
   cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde);
   cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil); cudaFree(e->d_shortw); cudaFree(e->d_win); cudaFree(e->d_cnt);
-  cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs);
+  cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
   cudaFree(e->d_ctr); cudaFree(e->d_status);
   for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);
   if (e->stream) cudaStreamDestroy(e->stream);

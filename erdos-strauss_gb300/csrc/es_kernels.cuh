@@ -75,7 +75,13 @@ struct MarkParams {
 // so that any 64 consecutive residues starting below s are one funnel shift of two words.
 constexpr u32 MASK_BYTES_MAX = 48 * 1024;   // per-lane mask table budget (shared memory)
 
-struct MaskDesc { u32 s, d, off, c64; };    // stride, its index in sdist, word offset, 64 mod s
+struct MaskDesc { u32 s, d, off, c32; };    // stride, its index in sdist, 32-bit word offset, 32 mod s
+
+// A short window as k_mark_short walks it: lanes outside [la, lb) have no position in it.
+struct ShortWin {
+  u64 Q, hi;
+  u32 lomod, wi, la, lb;
+};
 
 struct ShortParams {
   const u32 *rho;
@@ -86,7 +92,7 @@ struct ShortParams {
   const MaskDesc *mdesc;    // covers' mask strides [0, nm_cov), then stage B' [nm_cov, nm_all)
   const u32 *lfil;          // filters not covered by a mask: covers [0, nl_cov), then B' [nl_cov, nl_all)
   const WinDev *win;
-  const u32 *shortw;        // indices of the short windows
+  const ShortWin *shortw;   // the short windows
   Surv *surv;
   unsigned long long *surv_count;
   WinCount *cnt;
@@ -97,6 +103,8 @@ struct ShortParams {
 struct TailParams {
   Surv *surv;
   unsigned long long *surv_count;
+  u32 *cand;               // indices into surv that passed the base-2 round
+  unsigned long long *cand_count;
   u32 *primes;             // indices into surv
   unsigned long long *prime_count;
   u32 *direct;             // indices into surv, primes that no rung certified
