@@ -122,7 +122,7 @@ __constant__ const u64 MR_BASES[12] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 3
 
 // The reference's is_prime: trial division by the 12 bases, then all 12 SPRP rounds
 // (census/rung_scan.cpp:76-92). Deterministic for n < 3.3e24.
-__device__ bool is_prime64(u64 n) {
+__device__ inline bool is_prime64(u64 n) {
   if (n < 2) return false;
   #pragma unroll
   for (int i = 0; i < 12; ++i) {
@@ -139,7 +139,7 @@ __device__ bool is_prime64(u64 n) {
 }
 
 // Base-2 SPRP (sieve/rung_scan3.cpp:680-689) on an odd n > 2.
-__device__ bool sprp2_64(u64 n) {
+__device__ inline bool sprp2_64(u64 n) {
   if (n < 2) return false;
   if (!(n & 1)) return n == 2;
   const Mont M = mont_init(n);
@@ -179,7 +179,7 @@ __device__ __forceinline__ u64 isqrt64(u64 n) {
 // of |x - y| batched 128 at a time between gcds, a backtrack when the batch overshoots, and
 // the next c when the cycle closes without a split. The step budget is shared across c;
 // exhausting it sets ST_RHO_BUDGET and returns 0.
-__device__ u64 rho_split(u64 n, u64 &budget, u32 *status) {
+__device__ inline u64 rho_split(u64 n, u64 &budget, u32 *status) {
   if (!(n & 1)) return 2;
   const Mont M = mont_init(n);
   for (u64 c = 1; c < 4096; ++c) {
@@ -224,7 +224,7 @@ __device__ u64 rho_split(u64 n, u64 &budget, u32 *status) {
 // Factor a cofactor n > 2^32 that has no prime factor below 2^16. Such an n has at most
 // three prime factors (65537^4 > 2^64), so a stack of four pending composites suffices.
 // Returns false if a bound was hit.
-__device__ bool factor_hard(u64 n, Fac &f, u32 *status) {
+__device__ inline bool factor_hard(u64 n, Fac &f, u32 *status) {
   u64 stack[6];
   int sp = 0;
   stack[sp++] = n;
@@ -249,7 +249,7 @@ __device__ bool factor_hard(u64 n, Fac &f, u32 *status) {
 // The complete factorization of n >= 1 (factorA_fast, sieve/rung_scan3.cpp:410-431):
 // powers of 2, trial division by the odd primes below 2^16 while d^2 <= n, then the
 // cofactor (prime when <= 2^32, else factor_hard). Prime order is left as found.
-__device__ bool factor64(u64 n, Fac &f, const u32 *__restrict__ tdp,
+__device__ inline bool factor64(u64 n, Fac &f, const u32 *__restrict__ tdp,
                          const TdEntry *__restrict__ tde, u32 *status) {
   f.k = 0;
   if (n == 0) return true;
@@ -300,7 +300,7 @@ __device__ __forceinline__ bool mul_le(U128 a, u64 b, U128 q) {
 // (min_div_res, sieve/rung_scan3.cpp:544-565). cur[s] is the least divisor built so far in
 // residue class s; absorbing a prime power keeps per-residue minima, and a partial product
 // above q is never extended (v > q/pr is tested exactly as v*pr > q).
-__device__ U128 min_div_res(u64 p, const Fac &fA, U128 q, u32 r, u32 target) {
+__device__ inline U128 min_div_res(u64 p, const Fac &fA, U128 q, u32 r, u32 target) {
   U128 cur[RCAP + 1], nxt[RCAP + 1];
   const U128 INF{~0ull, ~0ull};
   for (u32 s = 0; s < r; ++s) cur[s] = INF;
@@ -331,7 +331,7 @@ __device__ U128 min_div_res(u64 p, const Fac &fA, U128 q, u32 r, u32 target) {
 // solve_rung3 (sieve/rung_scan3.cpp:578-603): the smallest rung r == -p (mod 4), r <= 255,
 // skipping gcd(q mod r, r) > 1, at which the DP finds a witness. Returns false when no
 // rung certifies p (or when a bound was hit: the status word says which).
-__device__ bool solve_rung(u64 p, u64 &A_out, u32 &r_out, U128 &u_out, const u32 *tdp,
+__device__ inline bool solve_rung(u64 p, u64 &A_out, u32 &r_out, U128 &u_out, const u32 *tdp,
                            const TdEntry *tde, u32 *status) {
   const u32 pm4 = (u32)(p & 3);
   const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
@@ -357,7 +357,7 @@ __device__ bool solve_rung(u64 p, u64 &A_out, u32 &r_out, U128 &u_out, const u32
 // solve_direct3 (sieve/rung_scan3.cpp:607-647): for a, d in 1..8 in that order, the least
 // divisor m of n = p + 4a^2 d with m == -1 (mod 4ad), c = (m+1)/(4ad), k = n/m, ck > a.
 // The reference sorts the divisors and takes the first hit; the least hit is the same.
-__device__ bool solve_direct(u64 p, u64 &a_out, u64 &c_out, u64 &d_out, u64 &k_out,
+__device__ inline bool solve_direct(u64 p, u64 &a_out, u64 &c_out, u64 &d_out, u64 &k_out,
                              const u32 *tdp, const TdEntry *tde, u32 *status) {
   for (u64 a = 1; a <= 8; ++a)
     for (u64 d = 1; d <= 8; ++d) {

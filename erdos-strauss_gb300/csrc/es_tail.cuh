@@ -43,7 +43,7 @@ __device__ __forceinline__ void wf_add(WarpFac &F, u64 p, int e, u32 lane) {
 
 // The 12-base deterministic test (census/rung_scan.cpp:76-92) with one base per lane.
 // All lanes must call; returns the same verdict in every lane.
-__device__ bool warp_is_prime(u64 n, u32 lane) {
+__device__ inline bool warp_is_prime(u64 n, u32 lane) {
   bool ok = true;
   if (n < 2) return false;
   if (n <= 37) {
@@ -68,7 +68,7 @@ __device__ bool warp_is_prime(u64 n, u32 lane) {
 
 // Brent's rho in every lane with its own constant; returns a nontrivial factor of the odd
 // composite n (the same value in every lane), or 0 when every lane exhausted its budget.
-__device__ u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
+__device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
   if (lane == 0) *found = 0;
   __syncwarp();
   const Mont M = mont_init(n);
@@ -121,7 +121,7 @@ __device__ u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
 
 // Complete factorization of n >= 1 into F (prime order as found). All lanes call.
 // Returns false when a bound was hit (status says which).
-__device__ bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
+__device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
                             u32 *status, u32 lane, volatile u64 *rho_slot) {
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
@@ -222,7 +222,7 @@ struct DPWarp {            // shared memory, one per warp
 
 // min_div_res (sieve/rung_scan3.cpp:544-565), lanes over residue classes. Returns the
 // least divisor u <= q of q^2 with u == target (mod r), or 0.
-__device__ U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, u32 target, DPWarp &D, u32 lane) {
+__device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, u32 target, DPWarp &D, u32 lane) {
   const U128 INF{~0ull, ~0ull};
   for (u32 t = lane; t < r; t += 32) D.cur[t] = (t == 1 % r) ? U128{1, 0} : INF;
   __syncwarp();
@@ -270,7 +270,7 @@ struct RungResult { u64 A; u32 r, k; U128 u; };
 // stops once k passes the best certifying index found by any warp. Returns true in every
 // thread when some rung certifies p; the block's result is then in *out.
 template <int W>
-__device__ bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
+__device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
                                  volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out) {
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) *best_k = 0x7FFFFFFF;

@@ -109,6 +109,7 @@ def load_library(path=LIB_PATH):
         "es_solve_rung_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(Record), P(C.c_uint8)]),
         "es_solve_direct_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(Record), P(C.c_uint8)]),
         "es_factor_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(C.c_uint64), P(C.c_uint8), P(C.c_uint8)]),
+        "es_is_prime_noalloc": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

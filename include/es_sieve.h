@@ -185,6 +185,22 @@ es_status es_solve_direct_batch(es_engine *engine, const uint64_t *p, size_t cou
 es_status es_factor_batch(es_engine *engine, const uint64_t *n, size_t count, uint64_t *pr,
                           uint8_t *ex, uint8_t *k);
 
+/* Primality of count values already on the device, for callers that cannot allocate
+ * device memory (a process whose device memory is all reserved up front, code where an
+ * allocation may not block or fail at run time, a framework that owns every allocation).
+ * No counterpart in the reference, which has no device path of its own for this.
+ * d_n and d_out are device pointers owned by the caller; out[i] = 1 when n[i] is prime
+ * (the verdict of es_is_prime_batch). The work is queued on `stream` (a cudaStream_t; NULL
+ * for the default stream) on the current device and the call returns without waiting.
+ * Its scratch is a fixed array of (ES_NOALLOC_MAX + 64) 32-bit words in the library's
+ * device image, held by every GPU that loads the library until the process exits; the call
+ * itself allocates nothing. count above ES_NOALLOC_MAX is refused with ES_ERR_ARG. The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress), so make it
+ * before any stream capture. Every call shares the one array: calls that overlap on the GPU
+ * (on different streams, or from different threads) race; serialise them. */
+#define ES_NOALLOC_MAX (1u << 20)
+es_status es_is_prime_noalloc(const uint64_t *d_n, size_t count, uint8_t *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
