@@ -36,6 +36,9 @@ import workloads  # noqa: E402
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
 METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
+# DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch, from the
+# ncu capture summarised in profiles/k_mark_short_batch4096_dram.md
+MARK_SHORT_TRAFFIC = None
 
 
 def parse():
@@ -222,20 +225,24 @@ def run_gpu(args, ws, rank, local):
     barrier(ws)
     dev_ms, wall_s, launches, recs_n, items = 0.0, 0.0, 0, 0, 0
     stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
+    kern = {"prep_ms": 0.0, "mark_short_ms": 0.0, "mark_long_ms": 0.0}
+    warr, carr = eng.make_windows(wins), eng.make_counters(len(wins))
     with Clocks(local) as clk:
         for _ in range(args.steps):
             flush()
             t0 = time.perf_counter()
-            per, recs = eng.run_batch(wins)
+            nrec = eng.run_batch_c(warr, len(wins), carr)     # es_run_batch: host buffers in and out
             wall_s += time.perf_counter() - t0
             t = eng.timing()
             last_t = t
             dev_ms += t["total_ms"]
             launches += int(t["kernel_launches"])
             items = int(t["mark_items"])
-            recs_n = len(recs)
+            recs_n = nrec
             for k in stage:
                 stage[k] += t[k]
+            for k in kern:
+                kern[k] += t[k]
     barrier(ws)
     clocks = clk.summary()
     dev_s = allmax(ws, dev_ms / 1000.0)
@@ -259,24 +266,24 @@ def run_gpu(args, ws, rank, local):
         t3 = eng.timing()
         extra["c3"] = {"value": (c3["hi"] - c3["lo"]) / (t3["total_ms"] / 1000.0), "ms_per_step": t3["total_ms"],
                        "lo": c3["lo"], "mark_ms": t3["mark_ms"], "rung_ms": t3["rung_ms"]}
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel (per-kernel CUDA events on the engine's stream)
     hbm, peak_kind = peaks()
-    dom = max(stage, key=stage.get)
-    info = eng.info()
-    L, ldk = info["lanes"], (info["n_filters"] + 7) // 8 * 8
-    mark_bytes = items * ldk * 2           # the K0 row each (window, lane, segment) item reads
-    per_launch_ms = stage[dom] / args.steps
-    if dom == "mark_ms":
-        achieved = mark_bytes / (per_launch_ms / 1000.0) / 1e9
-        roof = {"kernel": "k_mark", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
-                "algorithmic_bytes": mark_bytes}
+    per_kernel = {"k_mark_short": kern["mark_short_ms"], "k_mark": kern["mark_long_ms"], "k_prep": kern["prep_ms"],
+                  "k_mr": stage["mr_ms"], "k_rung": stage["rung_ms"], "k_direct": stage["direct_ms"]}
+    dom = max(per_kernel, key=per_kernel.get)
+    per_launch_ms = per_kernel[dom] / args.steps
+    if dom == "k_mark_short":
+        # one kill-mask row per lane from HBM, plus the per-window stride residues and window list
+        alg = last_t["mask_bytes"] + len(wins) * 263 * 2 + len(wins) * 32
+        traffic = MARK_SHORT_TRAFFIC
     else:
-        # the survivor tail reads a few bytes per prime: report it against HBM honestly
-        achieved = (recs_n * 64) / (per_launch_ms / 1000.0) / 1e9
-        roof = {"kernel": {"rung_ms": "k_rung", "mr_ms": "k_mr", "direct_ms": "k_direct"}[dom], "bound": "hbm",
-                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                "peak_kind": peak_kind, "note": "latency-bound integer tail; HBM is not its limit"}
+        # the survivor tail: 24 B in and 64 B out per prime
+        alg = int(last_t["primes"]) * (24 + 64)
+        traffic = None
+    achieved = alg / (per_launch_ms / 1000.0) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes": alg, "ms_per_launch": per_launch_ms,
+            "note": "issue-bound integer work: the HBM fraction is small by construction; see profiles/"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
@@ -289,10 +296,13 @@ def run_gpu(args, ws, rank, local):
                 "config": {"workload": "batch4096", "windows": args.windows, "integers_per_step": n_int,
                            "wheel": 2042040, "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED,
                            "schedule": "persistent", "l2": flush_note, "parallelism": "replicas x%d" % ws},
-                "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 * len(wins),
-                        "d2h_bytes_per_step": 64 * len(wins) + 64 * recs_n},
+                # copied every step: batch header, window and short-window descriptors in; run
+                # counters, status, per-window counters and records out (pinned staging)
+                "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),
+                        "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * recs_n},
                 "gpu_launches": launches, "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
-                "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},
+                "stages_ms_per_step": dict({k: v / args.steps for k, v in stage.items()},
+                                           **{k: v / args.steps for k, v in kern.items()}),
                 "tail": {"survivors": int(last_t["survivors"]), "primes": int(last_t["primes"])}}
         line.update(extra)
         print(json.dumps(line))

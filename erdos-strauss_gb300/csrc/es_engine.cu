@@ -139,12 +139,13 @@ struct ItemInfo {
 
 // Per-window residues (lo / M) mod s_d for every distinct stride: computed once per window
 // here, instead of once per (window, lane) item.
-__global__ void k_prep(const WinDev *__restrict__ win, u32 nwin, const u32 *__restrict__ sdist, u32 D,
-                       u16 *__restrict__ Qm) {
-  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (u64)nwin * D) return;
-  const u32 w = (u32)(idx / D), d = (u32)(idx % D);
-  Qm[idx] = (u16)(win[w].Q % sdist[d]);
+__global__ void k_prep(const BatchHdr *__restrict__ hdr, const WinDev *__restrict__ win,
+                       const u32 *__restrict__ sdist, u32 D, u16 *__restrict__ Qm) {
+  const u64 total = (u64)hdr->nwin * D;
+  for (u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (u64)gridDim.x * blockDim.x) {
+    const u32 w = (u32)(idx / D), d = (u32)(idx % D);
+    Qm[idx] = (u16)(win[w].Q % sdist[d]);
+  }
 }
 
 // Items are dealt from an atomic queue (persistent schedule: gridDim = resident CTAs) or
@@ -160,14 +161,16 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
   __shared__ u32 red[BLOCK / 32];
   __shared__ u64 s_item;
   const u32 lane_id = threadIdx.x & 31;
+  const u64 total_items = P.hdr->total_items;
+  const u32 nwin = P.hdr->nwin;
   u64 next = blockIdx.x;
   for (;;) {
     if (threadIdx.x == 0) {
       const u64 item = persistent ? atomicAdd(reinterpret_cast<unsigned long long *>(P.queue), 1ull) : next;
       s_item = item;
       it.valid = 0;
-      if (item < P.total_items) {
-        u32 lo = 0, hi = P.nwin;                   // last window with item0 <= item
+      if (item < total_items) {
+        u32 lo = 0, hi = nwin;                     // last window with item0 <= item
         while (hi - lo > 1) {
           const u32 mid = (lo + hi) >> 1;
           if (P.win[mid].item0 <= item) lo = mid; else hi = mid;
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
     }
     __syncthreads();
     const u64 item = s_item;
-    if (item >= P.total_items) break;
+    if (item >= total_items) break;
     next += gridDim.x;
     const u32 win = it.win, G = it.G, lane_base = it.lane_base;
     const u64 J0 = it.J0;
@@ -417,6 +420,7 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
   extern __shared__ __align__(16) u32 tab[];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (P.hdr->nshort == 0) return;
   for (u32 l = blockIdx.x; l < P.L; l += gridDim.x) {
     const uint4 *src = reinterpret_cast<const uint4 *>(P.mtab + (size_t)l * P.Wpad);
     uint4 *dst = reinterpret_cast<uint4 *>(tab);
@@ -424,7 +428,8 @@ __global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
     __syncthreads();
     const u64 rho = P.rho[l];
     const u16 *K0row = P.K0 + (size_t)l * P.ldk;
-    for (u32 i = warp; i < P.nshort; i += BLOCK / 32) {
+    const u32 nshort = P.hdr->nshort;
+    for (u32 i = warp; i < nshort; i += BLOCK / 32) {
       const ShortWin W = P.shortw[i];
       if (l < W.la || l >= W.lb) continue;
       const u32 b = rho < W.lomod ? 1u : 0u;
@@ -620,11 +625,6 @@ __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *
 constexpr int MARK_BLOCK = 128;
 constexpr int SHORT_BLOCK = 256;
 
-struct DevBuf {
-  void *p = nullptr;
-  size_t bytes = 0;
-};
-
 }  // namespace es
 
 struct es_engine {
@@ -641,7 +641,7 @@ struct es_engine {
   uint32_t nf = 0, ldk = 0, D = 0, Lpad = 0;
   int device = 0, sm_count = 0, mark_occupancy = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[12] = {};
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
   es::u16 *d_K0 = nullptr, *d_K0T = nullptr;
@@ -654,7 +654,17 @@ struct es_engine {
   size_t shortw_cap = 0;
   uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0;
   es::TdEntry *d_tde = nullptr;
-  // per-run buffers
+  // per-run buffers (device) and their pinned host staging
+  es::BatchHdr *d_hdr = nullptr, *h_hdr = nullptr;
+  es::WinDev *h_win = nullptr;
+  es::ShortWin *h_short = nullptr;
+  es::WinCount *h_cnt = nullptr;
+  unsigned long long *h_ctr = nullptr;
+  es::u32 *h_status = nullptr;
+  es::RecDev *h_recs = nullptr;
+  // the persistent schedule's launch sequence, captured once per buffer capacity
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
   es::WinDev *d_win = nullptr; size_t win_cap = 0;
   es::WinCount *d_cnt = nullptr;
   es::Surv *d_surv = nullptr;
@@ -682,52 +692,65 @@ static es_status fail(es_engine *e, es_status s, const std::string &msg) {
       return fail(e, ES_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));   \
   } while (0)
 
+static void drop_graph(es_engine *e) {
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  e->gexec = nullptr;
+  e->graph = nullptr;
+}
+
+// Device buffers for nwin windows and a survivor capacity of cap, with their pinned host
+// staging. Growing any of them invalidates the captured graph (its copies and kernel
+// parameters name the old buffers and sizes).
 static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
+  if (!e->d_hdr) {
+    CU(cudaMalloc(&e->d_hdr, sizeof(BatchHdr)));
+    CU(cudaMallocHost(&e->h_hdr, sizeof(BatchHdr)));
+    CU(cudaMallocHost(&e->h_ctr, 8 * sizeof(unsigned long long)));
+    CU(cudaMallocHost(&e->h_status, sizeof(u32)));
+  }
   if (nwin > e->win_cap) {
-    if (e->d_win) cudaFree(e->d_win);
-    if (e->d_cnt) cudaFree(e->d_cnt);
-    e->d_win = nullptr; e->d_cnt = nullptr;
-    size_t want = std::max<size_t>(nwin, 64);
+    drop_graph(e);
+    cudaFree(e->d_win); cudaFree(e->d_cnt); cudaFree(e->d_shortw); cudaFree(e->d_Qm);
+    cudaFreeHost(e->h_win); cudaFreeHost(e->h_short); cudaFreeHost(e->h_cnt);
+    e->d_win = nullptr; e->d_cnt = nullptr; e->d_shortw = nullptr; e->d_Qm = nullptr;
+    e->h_win = nullptr; e->h_short = nullptr; e->h_cnt = nullptr;
+    const size_t want = std::max<size_t>(nwin, 64);
     CU(cudaMalloc(&e->d_win, want * sizeof(WinDev)));
     CU(cudaMalloc(&e->d_cnt, want * sizeof(WinCount)));
-    e->win_cap = want;
-  }
-  if (nwin > e->shortw_cap) {
-    if (e->d_shortw) cudaFree(e->d_shortw);
-    e->d_shortw = nullptr;
-    const size_t want = std::max<size_t>(nwin, 64);
     CU(cudaMalloc(&e->d_shortw, want * sizeof(ShortWin)));
-    e->shortw_cap = want;
-  }
-  if ((size_t)nwin * e->D > e->qm_cap) {
-    if (e->d_Qm) cudaFree(e->d_Qm);
-    e->d_Qm = nullptr;
-    const size_t want = std::max<size_t>(nwin, 64) * std::max<u32>(e->D, 1);
-    CU(cudaMalloc(&e->d_Qm, want * sizeof(u16)));
-    e->qm_cap = want;
+    CU(cudaMalloc(&e->d_Qm, want * std::max<u32>(e->D, 1) * sizeof(u16)));
+    CU(cudaMallocHost(&e->h_win, want * sizeof(WinDev)));
+    CU(cudaMallocHost(&e->h_short, want * sizeof(ShortWin)));
+    CU(cudaMallocHost(&e->h_cnt, want * sizeof(WinCount)));
+    e->win_cap = e->shortw_cap = want;
+    e->qm_cap = want * std::max<u32>(e->D, 1);
   }
   if (cap > e->cap) {
+    drop_graph(e);
     cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
-    e->d_surv = nullptr; e->d_primes = e->d_direct = e->d_cand = nullptr; e->d_recs = nullptr;
+    cudaFreeHost(e->h_recs);
+    e->d_surv = nullptr; e->d_primes = e->d_direct = e->d_cand = nullptr; e->d_recs = nullptr; e->h_recs = nullptr;
     CU(cudaMalloc(&e->d_surv, cap * sizeof(Surv)));
     CU(cudaMalloc(&e->d_primes, cap * sizeof(u32)));
     CU(cudaMalloc(&e->d_direct, cap * sizeof(u32)));
     CU(cudaMalloc(&e->d_cand, cap * sizeof(u32)));
     CU(cudaMalloc(&e->d_recs, cap * sizeof(RecDev)));
+    CU(cudaMallocHost(&e->h_recs, cap * sizeof(RecDev)));
     e->cap = cap;
   }
   return ES_OK;
 }
 
-static MarkParams mark_params(const es_engine *e, u64 total_items, u32 nwin) {
+static MarkParams mark_params(const es_engine *e) {
   MarkParams P;
   P.rho = e->d_rho; P.K0 = e->d_K0; P.K0T = e->d_K0T; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
   P.Qm = e->d_Qm; P.Lpad = e->Lpad;
   P.win = e->d_win; P.queue = reinterpret_cast<u64 *>(e->d_ctr + 0);
   P.surv = e->d_surv; P.surv_count = e->d_ctr + 1; P.cnt = e->d_cnt;
-  P.total_items = total_items; P.surv_cap = e->cap; P.M = e->M;
+  P.hdr = e->d_hdr; P.surv_cap = e->cap; P.M = e->M;
   P.L = (u32)e->classes.size(); P.ldk = e->ldk; P.nf = e->nf; P.ncov = (u32)e->ncov;
-  P.D = e->D; P.nwin = nwin;
+  P.D = e->D;
   P.r_bytes = (4 * e->D + 15) & ~15u;
   return P;
 }
@@ -796,51 +819,82 @@ static u64 positions_in(const es_engine *e, u64 lo, u64 hi) {
   return (len / M) * e->classes.size() + part;
 }
 
-// One pass of the funnel over the windows described in d_win, counting into cnt.
-// `persistent` selects the queue-driven k_mark (grid = resident CTAs); otherwise one CTA
-// per item.
-static es_status launch_funnel(es_engine *e, u64 total_items, u32 nwin, u32 nshort, bool persistent, WinCount *cnt) {
-  MarkParams P = mark_params(e, total_items, nwin);
+// One pass of the funnel on the engine's stream: reset the counters, copy the batch header
+// and descriptors from pinned staging (ncopy windows), the marking kernels, the survivor
+// tail, and the copies of the run counters back to pinned memory. With `capture` the event
+// records are external graph nodes, so that the kernels can still be timed when the
+// sequence runs as a graph. `items_hint` sizes k_mark's grid for the plain schedule.
+static es_status enqueue_funnel(es_engine *e, bool persistent, WinCount *cnt, size_t ncopy, size_t nshort_copy,
+                                u64 items_hint, bool capture) {
+  MarkParams P = mark_params(e);
   TailParams T = tail_params(e);
   P.cnt = cnt;
   T.cnt = cnt;
-  const size_t smem = mark_smem(e);
-  CU(cudaMemsetAsync(e->d_ctr, 0, 8 * sizeof(unsigned long long), e->stream));
-  unsigned grid = persistent ? (unsigned)std::min<u64>(total_items, (u64)e->sm_count * e->mark_occupancy)
-                             : (unsigned)std::min<u64>(total_items, 0x7FFFFFFFull);
-  if (grid == 0) grid = 1;
-  CU(cudaEventRecord(e->ev[0], e->stream));
-  if (nwin && e->D) {
-    const u64 nq = (u64)nwin * e->D;
-    k_prep<<<(unsigned)((nq + 255) / 256), 256, 0, e->stream>>>(e->d_win, nwin, e->d_sdist, e->D, e->d_Qm);
-    CU(cudaGetLastError());
-  }
-  if (nshort) {
+  cudaStream_t st = e->stream;
+  auto rec = [&](int k) {
+    return capture ? cudaEventRecordWithFlags(e->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(e->ev[k], st);
+  };
+  CU(cudaMemsetAsync(e->d_ctr, 0, 8 * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), st));
+  CU(cudaMemcpyAsync(e->d_hdr, e->h_hdr, sizeof(BatchHdr), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(e->d_win, e->h_win, ncopy * sizeof(WinDev), cudaMemcpyHostToDevice, st));
+  if (nshort_copy) CU(cudaMemcpyAsync(e->d_shortw, e->h_short, nshort_copy * sizeof(ShortWin), cudaMemcpyHostToDevice, st));
+  CU(rec(0));
+  k_prep<<<e->sm_count * 4, 256, 0, st>>>(e->d_hdr, e->d_win, e->d_sdist, e->D, e->d_Qm);
+  CU(cudaGetLastError());
+  CU(rec(7));
+  {
     ShortParams S;
     S.rho = e->d_rho; S.K0 = e->d_K0; S.fdesc = e->d_fdesc; S.Qm = e->d_Qm; S.mtab = e->d_mtab;
     S.mdesc = e->d_mdesc; S.lfil = e->d_lfil; S.win = e->d_win; S.shortw = e->d_shortw;
     S.surv = e->d_surv; S.surv_count = e->d_ctr + 1; S.cnt = cnt; S.surv_cap = e->cap; S.M = e->M;
-    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad;
-    S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all; S.nshort = nshort;
-    k_mark_short<SHORT_BLOCK><<<S.L, SHORT_BLOCK, (size_t)e->Wpad * 8, e->stream>>>(S);
+    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad; S.hdr = e->d_hdr;
+    S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all;
+    k_mark_short<SHORT_BLOCK><<<S.L, SHORT_BLOCK, (size_t)e->Wpad * 8, st>>>(S);
     CU(cudaGetLastError());
   }
-  if (total_items) {
-    k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, smem, e->stream>>>(P, persistent ? 1 : 0);
-    CU(cudaGetLastError());
+  CU(rec(8));
+  const unsigned grid = persistent ? (unsigned)((u64)e->sm_count * e->mark_occupancy)
+                                   : (unsigned)std::max<u64>(1, std::min<u64>(items_hint, 0x7FFFFFFFull));
+  k_mark<MARK_BLOCK><<<grid, MARK_BLOCK, mark_smem(e), st>>>(P, persistent ? 1 : 0);
+  CU(cudaGetLastError());
+  CU(rec(1));
+  k_mr<<<e->sm_count * 2, 256, 0, st>>>(T);
+  CU(cudaGetLastError());
+  k_mr2<<<e->sm_count * 2, 256, 0, st>>>(T);
+  CU(cudaGetLastError());
+  CU(rec(2));
+  k_rung<<<e->sm_count * 6, RUNG_WARPS * 32, 0, st>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
+  CU(cudaGetLastError());
+  CU(rec(3));
+  k_direct<<<e->sm_count, 32, 0, st>>>(T);
+  CU(cudaGetLastError());
+  CU(rec(4));
+  CU(cudaMemcpyAsync(e->h_ctr, e->d_ctr, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(e->h_status, e->d_status, sizeof(u32), cudaMemcpyDeviceToHost, st));
+  return ES_OK;
+}
+
+// The persistent schedule as a CUDA graph: counters cleared, the whole staging area copied,
+// every kernel, and the counters copied back, captured once and replayed per batch.
+static es_status capture_graph(es_engine *e) {
+  drop_graph(e);
+  CU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  es_status s = ES_OK;
+  const cudaError_t m = cudaMemsetAsync(e->d_cnt, 0, e->win_cap * sizeof(WinCount), e->stream);
+  if (m == cudaSuccess) s = enqueue_funnel(e, true, e->d_cnt, e->win_cap, e->shortw_cap, 0, true);
+  if (m == cudaSuccess && s == ES_OK) {
+    const cudaError_t c2 = cudaMemcpyAsync(e->h_cnt, e->d_cnt, e->win_cap * sizeof(WinCount),
+                                           cudaMemcpyDeviceToHost, e->stream);
+    if (c2 != cudaSuccess) s = fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(c2));
   }
-  CU(cudaEventRecord(e->ev[1], e->stream));
-  k_mr<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
-  CU(cudaGetLastError());
-  k_mr2<<<e->sm_count * 2, 256, 0, e->stream>>>(T);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(e->ev[2], e->stream));
-  k_rung<<<e->sm_count * 6, RUNG_WARPS * 32, 0, e->stream>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(e->ev[3], e->stream));
-  k_direct<<<e->sm_count, 32, 0, e->stream>>>(T);
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(e->ev[4], e->stream));
+  cudaGraph_t g = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+  if (m != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(m));
+  if (s != ES_OK) { if (g) cudaGraphDestroy(g); return s; }
+  if (end != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(end));
+  e->graph = g;
+  CU(cudaGraphInstantiate(&e->gexec, g, 0));
   return ES_OK;
 }
 
@@ -875,72 +929,85 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
   std::vector<ShortWin> shortw;
   const u64 total_items = describe(e, w, n, wd, shortw);
   u64 positions_bound = 0;
-  for (const WinDev &d : wd) positions_bound += (u64)d.nseg * d.seg * d.groups * d.G;
+  for (size_t i = 0; i < n; ++i) positions_bound += positions_in(e, w[i].lo, w[i].hi);
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
   cap = std::max(cap, e->cap);
-  const bool one_pass = schedule == ES_SCHED_PERSISTENT || n == 1;
-  std::vector<WinCount> hc(n);
+  const bool persistent = schedule == ES_SCHED_PERSISTENT;
   std::vector<RecDev> hr;
   bool done = false;
   for (int attempt = 0; attempt < 4 && !done; ++attempt) {
     es_status s = ensure_capacity(e, n, cap);
     if (s) return s;
-    CU(cudaMemsetAsync(e->d_cnt, 0, n * sizeof(WinCount), e->stream));
-    CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), e->stream));
-    unsigned long long ctr[8] = {0};
-    double mark_ms = 0, mr_ms = 0, rung_ms = 0, direct_ms = 0;
+    double mark_ms = 0, mr_ms = 0, rung_ms = 0, direct_ms = 0, prep_ms = 0, short_ms = 0, long_ms = 0;
     u64 launches = 0, surv_max = 0, surv_total = 0, prime_total = 0;
+    u32 status = 0;
     hr.clear();
-    CU(cudaEventRecord(e->ev[5], e->stream));
-    for (size_t i = 0; i < (one_pass ? 1 : n); ++i) {
-      // Plain schedule: the same kernels, one launch sequence per window.
-      WinDev one = wd[i];
-      one.item0 = 0;
-      const u64 items = one_pass ? total_items : (u64)one.nseg * one.groups;
-      // plain schedule: this window's short-window entry (if any), re-indexed to window 0
-      ShortWin one_short{};
-      u32 nshort = 0;
-      if (one_pass) {
-        nshort = (u32)shortw.size();
-      } else {
-        for (const ShortWin &sw : shortw)
-          if (sw.wi == i) { one_short = sw; one_short.wi = 0; nshort = 1; break; }
-      }
-      CU(cudaMemcpyAsync(e->d_win, one_pass ? wd.data() : &one, (one_pass ? n : 1) * sizeof(WinDev),
-                         cudaMemcpyHostToDevice, e->stream));
-      if (nshort)
-        CU(cudaMemcpyAsync(e->d_shortw, one_pass ? shortw.data() : &one_short, nshort * sizeof(ShortWin),
-                           cudaMemcpyHostToDevice, e->stream));
-      s = launch_funnel(e, items, one_pass ? (u32)n : 1, nshort, schedule == ES_SCHED_PERSISTENT,
-                        e->d_cnt + (one_pass ? 0 : i));
-      if (s) return s;
-      launches += 5 + (nshort ? 1 : 0) + (items ? 1 : 0);
-      CU(cudaMemcpyAsync(ctr, e->d_ctr, sizeof ctr, cudaMemcpyDeviceToHost, e->stream));
-      CU(cudaStreamSynchronize(e->stream));
+    auto collect = [&]() -> es_status {   // after a pass: timings, counts, records
+      prep_ms += ev_ms(e->ev[0], e->ev[7]); short_ms += ev_ms(e->ev[7], e->ev[8]);
+      long_ms += ev_ms(e->ev[8], e->ev[1]);
       mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
       rung_ms += ev_ms(e->ev[2], e->ev[3]); direct_ms += ev_ms(e->ev[3], e->ev[4]);
+      const unsigned long long *ctr = e->h_ctr;
       surv_max = std::max<u64>(surv_max, ctr[1]);
       surv_total += ctr[1]; prime_total += ctr[2];
-      if (ctr[1] > e->cap) break;
-      const size_t base = hr.size();
-      hr.resize(base + ctr[4]);
-      if (ctr[4]) CU(cudaMemcpy(hr.data() + base, e->d_recs, ctr[4] * sizeof(RecDev), cudaMemcpyDeviceToHost));
-      if (!one_pass) for (size_t k = base; k < hr.size(); ++k) hr[k].win = (u32)i;
+      status |= *e->h_status;
+      if (ctr[1] > e->cap) return ES_OK;
+      const size_t nrec = (size_t)std::min<u64>(ctr[4], e->cap);
+      if (nrec) {
+        CU(cudaMemcpyAsync(e->h_recs, e->d_recs, nrec * sizeof(RecDev), cudaMemcpyDeviceToHost, e->stream));
+        CU(cudaStreamSynchronize(e->stream));
+        hr.insert(hr.end(), e->h_recs, e->h_recs + nrec);
+      }
+      return ES_OK;
+    };
+    if (persistent) {
+      e->h_hdr->total_items = total_items;
+      e->h_hdr->nwin = (u32)n;
+      e->h_hdr->nshort = (u32)shortw.size();
+      memcpy(e->h_win, wd.data(), n * sizeof(WinDev));
+      if (!shortw.empty()) memcpy(e->h_short, shortw.data(), shortw.size() * sizeof(ShortWin));
+      if (!e->gexec) { s = capture_graph(e); if (s) return s; }
+      CU(cudaGraphLaunch(e->gexec, e->stream));
+      CU(cudaStreamSynchronize(e->stream));
+      launches = 7;
+      s = collect();
+      if (s) return s;
+    } else {
+      // The plain schedule: the same kernels, one launch sequence per window.
+      CU(cudaMemsetAsync(e->d_cnt, 0, n * sizeof(WinCount), e->stream));
+      size_t k = 0;                      // next short-window entry (describe emits them in order)
+      for (size_t i = 0; i < n; ++i) {
+        e->h_win[0] = wd[i];
+        e->h_win[0].item0 = 0;
+        const u64 items = (u64)wd[i].nseg * wd[i].groups;
+        u32 nshort = 0;
+        if (k < shortw.size() && shortw[k].wi == i) { e->h_short[0] = shortw[k++]; e->h_short[0].wi = 0; nshort = 1; }
+        e->h_hdr->total_items = items; e->h_hdr->nwin = 1; e->h_hdr->nshort = nshort;
+        s = enqueue_funnel(e, false, e->d_cnt + i, 1, nshort, items, false);
+        if (s) return s;
+        CU(cudaStreamSynchronize(e->stream));
+        launches += 7;
+        const size_t base = hr.size();
+        s = collect();
+        if (s) return s;
+        if (surv_max > e->cap) break;
+        for (size_t r = base; r < hr.size(); ++r) hr[r].win = (u32)i;
+      }
+      CU(cudaMemcpyAsync(e->h_cnt, e->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost, e->stream));
+      CU(cudaStreamSynchronize(e->stream));
     }
-    CU(cudaEventRecord(e->ev[6], e->stream));
-    CU(cudaStreamSynchronize(e->stream));
     if (surv_max > e->cap) {            // overflow: grow to the exact need and re-run
       cap = (size_t)(surv_max + surv_max / 4 + 1024);
       continue;
     }
-    u32 st = 0;
-    CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
-    if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
-    CU(cudaMemcpy(hc.data(), e->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost));
+    if (status) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(status));
     e->timing.total_ms = mark_ms + mr_ms + rung_ms + direct_ms;   // kernels only, inputs resident
     e->timing.mark_ms = mark_ms; e->timing.mr_ms = mr_ms;
+    e->timing.prep_ms = prep_ms; e->timing.mark_short_ms = short_ms; e->timing.mark_long_ms = long_ms;
+    e->timing.short_pairs = (u64)shortw.size() * e->classes.size();
+    e->timing.mask_bytes = shortw.empty() ? 0 : (u64)e->classes.size() * e->Wpad * 8;
     e->timing.rung_ms = rung_ms; e->timing.direct_ms = direct_ms;
-    e->timing.marks_kernel_launches = one_pass ? 1 : n;
+    e->timing.marks_kernel_launches = persistent ? 1 : n;
     e->timing.kernel_launches = launches;
     e->timing.mark_items = total_items;
     e->timing.survivors = surv_total;
@@ -949,10 +1016,9 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
   }
   if (!done) return fail(e, ES_ERR_NOMEM, "survivor list kept overflowing");
   for (size_t i = 0; i < n; ++i) {      // the SUMMARY counters (sieve/rung_scan3.cpp:764-772)
-    const WinCount &c = hc[i];
+    const WinCount &c = e->h_cnt[i];
     es_counters &o = per_window[i];
     o.positions = positions_in(e, w[i].lo, w[i].hi);
-    (void)c.positions;
     if (e->nf == e->ncov) { o.covered = o.positions - c.surv; o.sieved = 0; }
     else { o.covered = o.positions - c.after_covers; o.sieved = c.after_covers - c.surv; }
     o.mr = c.surv; o.composite = c.composite; o.rung = c.rung; o.direct = c.direct;
@@ -1282,7 +1348,10 @@ es_status es_close(es_engine *e) {
   cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde);
   cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil); cudaFree(e->d_shortw); cudaFree(e->d_win); cudaFree(e->d_cnt);
   cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
-  cudaFree(e->d_ctr); cudaFree(e->d_status);
+  cudaFree(e->d_ctr); cudaFree(e->d_status); cudaFree(e->d_hdr);
+  drop_graph(e);
+  cudaFreeHost(e->h_hdr); cudaFreeHost(e->h_win); cudaFreeHost(e->h_short); cudaFreeHost(e->h_cnt);
+  cudaFreeHost(e->h_ctr); cudaFreeHost(e->h_status); cudaFreeHost(e->h_recs);
   for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;

@@ -31,6 +31,13 @@ struct WinDev {
   u32 groups;     // lane groups per segment
 };
 
+// Sizes of the batch in flight, read by the marking kernels from device memory so that one
+// captured launch sequence (a CUDA graph) serves every batch up to the buffers' capacity.
+struct BatchHdr {
+  u64 total_items;   // long-window marking items
+  u32 nwin, nshort;  // windows; short windows
+};
+
 // A position that no filter killed: (window, lane, J) is its key in the output order.
 struct Surv {
   u64 p;
@@ -62,10 +69,10 @@ struct MarkParams {
   Surv *surv;              // survivor list
   unsigned long long *surv_count;
   WinCount *cnt;           // [nwin]
-  u64 total_items;
+  const BatchHdr *hdr;     // total_items, nwin
   u64 surv_cap;
   u64 M;
-  u32 L, Lpad, ldk, nf, ncov, D, nwin;
+  u32 L, Lpad, ldk, nf, ncov, D;
   u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
 };
 
@@ -97,7 +104,8 @@ struct ShortParams {
   unsigned long long *surv_count;
   WinCount *cnt;
   u64 surv_cap, M;
-  u32 L, ldk, D, Wpad, nm_cov, nm_all, nl_cov, nl_all, nshort;
+  const BatchHdr *hdr;      // nshort
+  u32 L, ldk, D, Wpad, nm_cov, nm_all, nl_cov, nl_all;
 };
 
 struct TailParams {

@@ -70,9 +70,10 @@ class Info(C.Structure):
 
 
 class Timing(C.Structure):
-    _fields_ = [(n, C.c_double) for n in ("total_ms", "mark_ms", "mr_ms", "rung_ms", "direct_ms")] + \
+    _fields_ = [(n, C.c_double) for n in ("total_ms", "mark_ms", "mr_ms", "rung_ms", "direct_ms", "prep_ms",
+                                          "mark_short_ms", "mark_long_ms")] + \
                [(n, C.c_uint64) for n in ("marks_kernel_launches", "kernel_launches", "mark_items", "survivors",
-                                          "primes")]
+                                          "primes", "short_pairs", "mask_bytes")]
 
 
 _lib = None
@@ -229,6 +230,24 @@ class Engine:
         r = Records()
         self._check(self.lib.es_run_batch(self.h, w, n, schedule, c, C.byref(r) if records else None))
         return [c[i].as_dict() for i in range(n)], (self._take_records(self.lib, r) if records else None)
+
+    # The C call alone, for timing: caller-built window and counter arrays (make_windows,
+    # make_counters), records freed here; returns the record count.
+    @staticmethod
+    def make_windows(windows):
+        n = len(windows)
+        return (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+
+    @staticmethod
+    def make_counters(n):
+        return (Counters * max(n, 1))()
+
+    def run_batch_c(self, warr, n, carr, schedule=ES_SCHED_PERSISTENT):
+        r = Records()
+        self._check(self.lib.es_run_batch(self.h, warr, n, schedule, carr, C.byref(r)))
+        nrec = r.n
+        self.lib.es_free_records(C.byref(r))
+        return nrec
 
     def summary(self, lo, hi, counters):
         c = Counters(*[counters[n] for n in COUNTER_NAMES])

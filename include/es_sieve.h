@@ -114,8 +114,11 @@ typedef struct {
  * total_ms is the sum of the stages (kernels only: no host<->device copies). */
 typedef struct {
   double total_ms, mark_ms, mr_ms, rung_ms, direct_ms;
+  double prep_ms, mark_short_ms, mark_long_ms;   /* the three parts of mark_ms */
   uint64_t marks_kernel_launches, kernel_launches;
   uint64_t mark_items, survivors, primes;
+  uint64_t short_pairs;     /* (lane, short window) pairs, active or not, walked by k_mark_short */
+  uint64_t mask_bytes;      /* kill-mask table bytes one k_mark_short launch reads */
 } es_timing_t;
 
 /* Batch schedules: per-window launches of the same kernels, or one persistent launch over

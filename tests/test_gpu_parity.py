@@ -241,3 +241,25 @@ def test_solve_direct_vs_oracle_small():
     ps = _primes_at(10 ** 9, 100) + _primes_at(10 ** 17, 50)
     got = engine().solve_direct(ps)
     assert got == [oracle.solve_direct(p) for p in ps]
+
+
+def test_every_emitted_certificate_rechecks_in_exact_arithmetic():
+    """The reference's exact-rational gate (sieve/verify_covers.py), restated in
+    oracle/verify.py, over everything the engine emits for a spread of windows."""
+    import verify
+    total = 0
+    cases = [(engine(), workloads.c3()["lo"], workloads.c3()["hi"]),
+             (engine(), 5000000000000000000, 5000001000000000000),
+             (engine(120120, None, mmax=200, no_rung=True), 1000000000000, 1000200000000),
+             (engine(2042040, GPU_TABLE, sieve_p=500), workloads.DIRECT_PMAX - (1 << 32), workloads.DIRECT_PMAX)]
+    for e, lo, hi in cases:
+        r, s_, bad, surv = verify.check_text(e.stream(lo, hi))
+        assert bad == 0 and surv == 0
+        total += r + s_
+    wins, _ = _batch48()
+    per, recs = engine().run_batch(wins)
+    for i, (lo, hi) in enumerate(wins):
+        r, s_, bad, surv = verify.check_text(engine().text(lo, hi, per[i], recs[recs["window"] == i]))
+        assert bad == 0 and surv == 0
+        total += r + s_
+    assert total > 9000

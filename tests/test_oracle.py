@@ -152,3 +152,18 @@ def test_reference_binaries_regenerate_fixtures():
                         "--filters", golden("filters", "f_M120120_mmax2000_runtime.txt")],
                        capture_output=True, text=True)
     assert r.stdout == read("gen", "c1_runtime.out")
+
+
+def test_certificate_checker_on_reference_records():
+    """The exact re-check accepts every certificate the reference emitted and rejects a
+    planted mistake (planted here, on the CPU, in a copy of a line)."""
+    import verify
+    for name in ("windows/w19_certificates.txt", "gen/d3_120120_m200_norung_cover_scan.out", "gen/c3_gpu.out"):
+        r, s_, bad, surv = verify.check_text(read(*name.split("/")))
+        assert bad == 0 and surv == 0 and r + s_ > 0
+    line = read("gen", "c3_gpu.out").splitlines()[0].split()
+    line[4] = str(int(line[4]) + 1)                       # a wrong witness u
+    assert verify.check_line(" ".join(line)) == ("RUNG", False)
+    sl = read("gen", "d3_120120_m200_norung_cover_scan.out").splitlines()[0].split()
+    sl[5] = str(int(sl[5]) + 1)                           # a wrong k
+    assert verify.check_line(" ".join(sl)) == ("SOLVED", False)
