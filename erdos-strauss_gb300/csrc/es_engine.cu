@@ -309,46 +309,65 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 }
 
 // ---------------------------------------------------------------- short windows
-// kill[c] gets bit j set when position 32c + j of the lane segment (n <= SEG_SMALL positions,
-// first K congruent to Qrow[d] + b modulo each stride) is killed by a mask stride in [m0, m1)
-// or by a filter of lfil[l0, l1). Lanes of the warp split the strides; the caller reduces.
-// Mask bits come out 32 at a time: word r/32 and the next, funnel-shifted right by r mod 32.
+// A CTA holds the kill-mask tables of SHORT_LANES consecutive lanes in shared memory; each
+// warp takes one short window at a time and marks the segments of those lanes in it. The
+// per-window work that does not depend on the lane -- the stride descriptor and the
+// segment-start residue (lo / M) mod s -- is done once for all SHORT_LANES lanes.
+constexpr int SHORT_LANES = 2;
+constexpr u32 SMD_MAX = 512;       // stride descriptors staged in shared memory
+
+// kill[q][c] gets bit j set when position 32c + j of lane q's segment is killed by a mask
+// stride in [m0, m1) or by a filter of lfil[l0, l1). A segment starts at K == Qrow[d] + b[q]
+// (mod s_d) and has n[q] positions (0: lane inactive). Mask bits come out 32 at a time: word
+// r/32 and the next, funnel-shifted right by r mod 32. Lanes of the warp split the strides;
+// the caller reduces.
 template <int NC>
-__device__ __forceinline__ void short_kill(u32 (&kill)[NC], u32 n, u32 b, const u32 *tab,
-                                           const MaskDesc *__restrict__ mdesc, u32 m0, u32 m1,
-                                           const u32 *__restrict__ lfil, u32 l0, u32 l1,
-                                           const u16 *__restrict__ K0row, const u32 *__restrict__ fdesc,
+__device__ __forceinline__ void short_kill(u32 (&kill)[SHORT_LANES][NC], const u32 (&n)[SHORT_LANES],
+                                           const u32 (&b)[SHORT_LANES], const u32 *tab, u32 tab_words,
+                                           const MaskDesc *smd, const MaskDesc *__restrict__ mdesc, u32 m0,
+                                           u32 m1, const u32 *__restrict__ lfil, u32 l0, u32 l1,
+                                           const u16 *const (&K0row)[SHORT_LANES], const u32 *__restrict__ fdesc,
                                            const u16 *__restrict__ Qrow, u32 lane) {
   for (u32 k = m0 + lane; k < m1; k += 32) {
-    const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k);
-    const MaskDesc md{mv.x, mv.y, mv.z, mv.w};
+    MaskDesc md;
+    if (smd) md = smd[k];
+    else { const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k); md = MaskDesc{mv.x, mv.y, mv.z, mv.w}; }
     const u32 s = md.s;
-    u32 r = (u32)__ldg(Qrow + md.d) + b;
-    r = r >= s ? r - s : r;
+    const u32 q0 = (u32)__ldg(Qrow + md.d);
     #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const u32 *wp = tab + md.off + (r >> 5);
-      kill[c] |= __funnelshift_r(wp[0], wp[1], r & 31);
-      if (c + 1 < NC) {
-        r += md.c32;
-        r = r >= s ? r - s : r;
+    for (int q = 0; q < SHORT_LANES; ++q) {
+      u32 r = q0 + b[q];
+      r = r >= s ? r - s : r;
+      const u32 *t = tab + q * tab_words + md.off;
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const u32 *wp = t + (r >> 5);
+        kill[q][c] |= __funnelshift_r(wp[0], wp[1], r & 31);
+        if (c + 1 < NC) {
+          r += md.c32;
+          r = r >= s ? r - s : r;
+        }
       }
     }
   }
   for (u32 k = l0 + lane; k < l1; k += 32) {
     const u32 f = lfil[k];
-    const u32 k0 = K0row[f];
-    if (k0 == K0_MISS) continue;
     const u32 fd = __ldg(fdesc + f);
     const u32 s = fd & 0xFFFFu;
-    u32 r = (u32)__ldg(Qrow + (fd >> 16)) + b;
-    r = r >= s ? r - s : r;
-    int off = (int)k0 - (int)r;
-    if (off < 0) off += (int)s;
-    for (u32 j = (u32)off; j < n; j += s) {
-      #pragma unroll
-      for (int c = 0; c < NC; ++c)
-        if ((j >> 5) == (u32)c) kill[c] |= 1u << (j & 31);
+    const u32 q0 = (u32)__ldg(Qrow + (fd >> 16));
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q) {
+      const u32 k0 = K0row[q][f];
+      if (k0 == K0_MISS) continue;
+      u32 r = q0 + b[q];
+      r = r >= s ? r - s : r;
+      int off = (int)k0 - (int)r;
+      if (off < 0) off += (int)s;
+      for (u32 j = (u32)off; j < n[q]; j += s) {
+        #pragma unroll
+        for (int c = 0; c < NC; ++c)
+          if ((j >> 5) == (u32)c) kill[q][c] |= 1u << (j & 31);
+      }
     }
   }
 }
@@ -359,92 +378,127 @@ __device__ __forceinline__ u32 warp_or32(u32 v) {
   return v;
 }
 
-// One lane segment of one short window, NC 32-position chunks (n <= 32 * NC).
+// The segments of SHORT_LANES lanes in one short window, NC 32-position chunks each.
 template <int NC>
-__device__ __forceinline__ void short_segment(const ShortParams &P, const u32 *tab, u32 l, u32 wi, u64 first,
-                                              u32 n, u32 b, const u16 *K0row, u32 lane) {
+__device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *tab, u32 tab_words,
+                                               const MaskDesc *smd, u32 l_first, u32 wi,
+                                               const u64 (&first)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
+                                               const u32 (&b)[SHORT_LANES], const u16 *const (&K0row)[SHORT_LANES],
+                                               u32 lane) {
   const u16 *Qrow = P.Qm + (size_t)wi * P.D;
-  u32 kill[NC];
+  u32 kill[SHORT_LANES][NC];
   #pragma unroll
-  for (int c = 0; c < NC; ++c) kill[c] = 0;
-  short_kill<NC>(kill, n, b, tab, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow, lane);
-  u32 alive[NC];
+  for (int q = 0; q < SHORT_LANES; ++q)
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) kill[q][c] = 0;
+  short_kill<NC>(kill, n, b, tab, tab_words, smd, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow,
+                 lane);
+  u32 alive[SHORT_LANES][NC];
   u32 cnt = 0;
   #pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    const u32 lo = 32 * c;
-    const u32 valid = n >= lo + 32 ? ~0u : (n > lo ? (1u << (n - lo)) - 1 : 0u);
-    alive[c] = valid & ~warp_or32(kill[c]);
-    cnt += __popc(alive[c]);
-  }
+  for (int q = 0; q < SHORT_LANES; ++q)
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const u32 lo = 32 * c;
+      const u32 valid = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
+      alive[q][c] = valid & ~warp_or32(kill[q][c]);
+      cnt += __popc(alive[q][c]);
+    }
   if (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov) {                  // stage B'
     if (lane == 0 && cnt) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
     #pragma unroll
-    for (int c = 0; c < NC; ++c) kill[c] = 0;
-    short_kill<NC>(kill, n, b, tab, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all, K0row, P.fdesc, Qrow,
-                   lane);
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) kill[q][c] = 0;
+    short_kill<NC>(kill, n, b, tab, tab_words, smd, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all,
+                   K0row, P.fdesc, Qrow, lane);
     cnt = 0;
     #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      alive[c] &= ~warp_or32(kill[c]);
-      cnt += __popc(alive[c]);
-    }
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        alive[q][c] &= ~warp_or32(kill[q][c]);
+        cnt += __popc(alive[q][c]);
+      }
   }
   if (cnt && lane == 0) {              // survivors are rare: lane 0 writes them in order
     u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
     atomicAdd(&P.cnt[wi].surv, (unsigned long long)cnt);
     #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      u32 x = alive[c];
-      while (x) {
-        const u32 k = __ffs(x) - 1;
-        x &= x - 1;
-        if (slot < P.surv_cap) {
-          const u64 J = 32 * c + k;
-          Surv sv;
-          sv.p = first + P.M * J;
-          sv.J = J;
-          sv.win = wi;
-          sv.lane = l;
-          P.surv[slot] = sv;
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        u32 x = alive[q][c];
+        while (x) {
+          const u32 k = __ffs(x) - 1;
+          x &= x - 1;
+          if (slot < P.surv_cap) {
+            const u64 J = 32 * c + k;
+            Surv sv;
+            sv.p = first[q] + P.M * J;
+            sv.J = J;
+            sv.win = wi;
+            sv.lane = l_first + q;
+            P.surv[slot] = sv;
+          }
+          ++slot;
         }
-        ++slot;
       }
-    }
   }
 }
 
-// One CTA per lane: the lane's kill-mask table is staged in shared memory with 128-bit
-// loads, then each warp takes short windows in turn and marks the lane's segment in them.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_mark_short(const ShortParams P) {
+__global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
   extern __shared__ __align__(16) u32 tab[];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (P.hdr->nshort == 0) return;
-  for (u32 l = blockIdx.x; l < P.L; l += gridDim.x) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(P.mtab + (size_t)l * P.Wpad);
-    uint4 *dst = reinterpret_cast<uint4 *>(tab);
-    for (u32 i = threadIdx.x; i < P.Wpad / 2; i += BLOCK) dst[i] = __ldg(src + i);
+  const u32 tab_words = P.Wpad * 2;                    // 32-bit words per lane table
+  MaskDesc *smd = nullptr;
+  if (P.nm_all <= SMD_MAX) {
+    smd = reinterpret_cast<MaskDesc *>(tab + SHORT_LANES * tab_words);
+    for (u32 k = threadIdx.x; k < P.nm_all; k += BLOCK) smd[k] = P.mdesc[k];
+  }
+  const u32 nshort = P.hdr->nshort;
+  for (u32 l0 = blockIdx.x * SHORT_LANES; l0 < P.L; l0 += gridDim.x * SHORT_LANES) {
+    for (int q = 0; q < SHORT_LANES; ++q) {
+      const u32 l = min(l0 + q, P.L - 1);              // a missing last lane loads a copy; it stays inactive
+      const uint4 *src = reinterpret_cast<const uint4 *>(P.mtab + (size_t)l * P.Wpad);
+      uint4 *dst = reinterpret_cast<uint4 *>(tab + q * tab_words);
+      for (u32 i = threadIdx.x; i < P.Wpad / 2; i += BLOCK) dst[i] = __ldg(src + i);
+    }
     __syncthreads();
-    const u64 rho = P.rho[l];
-    const u16 *K0row = P.K0 + (size_t)l * P.ldk;
-    const u32 nshort = P.hdr->nshort;
+    u64 rho[SHORT_LANES];
+    const u16 *K0row[SHORT_LANES];
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q) {
+      const u32 l = min(l0 + q, P.L - 1);
+      rho[q] = P.rho[l];
+      K0row[q] = P.K0 + (size_t)l * P.ldk;
+    }
     for (u32 i = warp; i < nshort; i += BLOCK / 32) {
       const ShortWin W = P.shortw[i];
-      if (l < W.la || l >= W.lb) continue;
-      const u32 b = rho < W.lomod ? 1u : 0u;
-      const u64 first = rho + P.M * (W.Q + b);
-      if (first >= W.hi) continue;
-      const u32 n = (u32)((W.hi - first - 1) / P.M + 1);
-      switch ((n + 31) >> 5) {
-        case 1: short_segment<1>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 2: short_segment<2>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 3: short_segment<3>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 4: short_segment<4>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 5: short_segment<5>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 6: short_segment<6>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        case 7: short_segment<7>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
-        default: short_segment<8>(P, tab, l, W.wi, first, n, b, K0row, lane); break;
+      u64 first[SHORT_LANES];
+      u32 n[SHORT_LANES], b[SHORT_LANES];
+      u32 nmax = 0;
+      #pragma unroll
+      for (int q = 0; q < SHORT_LANES; ++q) {
+        const u32 l = l0 + q;
+        b[q] = rho[q] < W.lomod ? 1u : 0u;
+        first[q] = rho[q] + P.M * (W.Q + b[q]);
+        n[q] = (l < P.L && l >= W.la && l < W.lb && first[q] < W.hi)
+                   ? (u32)((W.hi - first[q] - 1) / P.M + 1) : 0u;
+        nmax = max(nmax, n[q]);
+      }
+      if (nmax == 0) continue;
+      switch ((nmax + 31) >> 5) {
+        case 1: short_segments<1>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 2: short_segments<2>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 3: short_segments<3>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 4: short_segments<4>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 5: short_segments<5>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 6: short_segments<6>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 7: short_segments<7>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        default: short_segments<8>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
       }
     }
     __syncthreads();
@@ -767,6 +821,10 @@ static TailParams tail_params(const es_engine *e) {
   return T;
 }
 
+static size_t short_smem(const es_engine *e) {
+  return (size_t)SHORT_LANES * e->Wpad * 8 + (e->nm_all <= SMD_MAX ? e->nm_all * sizeof(MaskDesc) : 0);
+}
+
 static size_t mark_smem(const es_engine *e) {
   return ((4 * e->D + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
 }
@@ -850,7 +908,7 @@ static es_status enqueue_funnel(es_engine *e, bool persistent, WinCount *cnt, si
     S.surv = e->d_surv; S.surv_count = e->d_ctr + 1; S.cnt = cnt; S.surv_cap = e->cap; S.M = e->M;
     S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad; S.hdr = e->d_hdr;
     S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all;
-    k_mark_short<SHORT_BLOCK><<<S.L, SHORT_BLOCK, (size_t)e->Wpad * 8, st>>>(S);
+    k_mark_short<SHORT_BLOCK><<<(S.L + SHORT_LANES - 1) / SHORT_LANES, SHORT_BLOCK, short_smem(e), st>>>(S);
     CU(cudaGetLastError());
   }
   CU(rec(8));
@@ -1186,7 +1244,7 @@ static es_status build_tables(es_engine *e) {
     CU(cudaStreamSynchronize(e->stream));
     cudaFree(d_fmask);
     CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(MASK_BYTES_MAX + 16)));
+                            (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc))));
   }
   CU(cudaStreamSynchronize(e->stream));
   cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
