@@ -338,15 +338,15 @@ __device__ __forceinline__ void short_kill(u32 (&kill)[SHORT_LANES][NC], const u
     for (int q = 0; q < SHORT_LANES; ++q) {
       u32 r = q0 + b[q];
       r = r >= s ? r - s : r;
-      const u32 *t = tab + q * tab_words + md.off;
+      // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
+      const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+      const u32 sh = r & 31;
+      u32 w0 = wp[0];
       #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const u32 *wp = t + (r >> 5);
-        kill[q][c] |= __funnelshift_r(wp[0], wp[1], r & 31);
-        if (c + 1 < NC) {
-          r += md.c32;
-          r = r >= s ? r - s : r;
-        }
+        const u32 w1 = wp[c + 1];
+        kill[q][c] |= __funnelshift_r(w0, w1, sh);
+        w0 = w1;
       }
     }
   }
@@ -372,11 +372,7 @@ __device__ __forceinline__ void short_kill(u32 (&kill)[SHORT_LANES][NC], const u
   }
 }
 
-__device__ __forceinline__ u32 warp_or32(u32 v) {
-  #pragma unroll
-  for (int o = 16; o; o >>= 1) v |= __shfl_xor_sync(0xFFFFFFFFu, v, o);
-  return v;
-}
+__device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFFFFFFu, v); }
 
 // The segments of SHORT_LANES lanes in one short window, NC 32-position chunks each.
 template <int NC>
@@ -506,8 +502,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
 }
 
 // Kill masks from the first-hit table: bit x of lane l's mask for filter f's stride, for
-// every x == K0[l][f] (mod s) below s + 32 (the repeat that a 32-bit window starting below s
-// may reach).
+// every x == K0[l][f] (mod s) below s + SEG_SMALL (the repeat that a segment of up to
+// SEG_SMALL positions starting below s may reach).
 __global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf, const int *__restrict__ fmask,
                               const MaskDesc *__restrict__ mdesc, u32 Wpad, u64 *__restrict__ mtab) {
   const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -519,7 +515,7 @@ __global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf
   if (k0 == K0_MISS) return;
   const MaskDesc md = mdesc[m];
   u32 *row = reinterpret_cast<u32 *>(mtab + (size_t)l * Wpad) + md.off;
-  for (u32 x = k0; x < md.s + 32; x += md.s) atomicOr(row + (x >> 5), 1u << (x & 31));
+  for (u32 x = k0; x < md.s + SEG_SMALL; x += md.s) atomicOr(row + (x >> 5), 1u << (x & 31));
 }
 
 // Miller-Rabin in two passes. Nearly every survivor is composite and fails the base-2
@@ -1204,9 +1200,9 @@ static es_status build_tables(es_engine *e) {
       strides.erase(std::unique(strides.begin(), strides.end()), strides.end());
       std::vector<int> slot_of(65536, -1);
       for (u32 st : strides) {
-        // bits [0, s + 32) plus one spare word, so that the second word of a window that starts
-        // at any residue below s is inside the stride's slice
-        const u32 wd = (st + 32 + 31) / 32 + 1;
+        // bits [0, s + SEG_SMALL) plus one spare word: a segment of up to SEG_SMALL positions
+        // starting at any residue below s reads words r/32 .. r/32 + SEG_SMALL/32 of the slice
+        const u32 wd = (st + SEG_SMALL + 31) / 32 + 1;
         if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX) break;
         const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
         slot_of[st] = (int)md.size();

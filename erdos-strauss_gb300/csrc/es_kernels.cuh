@@ -78,8 +78,9 @@ struct MarkParams {
 
 // Short windows (at most SEG_SMALL positions in any lane) are marked from per-(lane, stride)
 // kill masks: for lane l and a stride s shared by several filters, bit x of the mask is set
-// when some filter of that stride kills K == x (mod s); bits [s, s + 64) repeat the pattern
-// so that any 64 consecutive residues starting below s are one funnel shift of two words.
+// when some filter of that stride kills K == x (mod s); bits [s, s + SEG_SMALL) repeat the
+// pattern so that the positions of a whole segment starting below s are consecutive bits,
+// read 32 at a time as funnel shifts of consecutive words.
 constexpr u32 MASK_BYTES_MAX = 48 * 1024;   // per-lane mask table budget (shared memory)
 
 struct MaskDesc { u32 s, d, off, c32; };    // stride, its index in sdist, 32-bit word offset, 32 mod s
