@@ -479,13 +479,15 @@ __global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
       #pragma unroll
       for (int q = 0; q < SHORT_LANES; ++q) {
         const u32 l = l0 + q;
-        b[q] = rho[q] < W.lomod ? 1u : 0u;
-        first[q] = rho[q] + P.M * (W.Q + b[q]);
-        n[q] = (l < P.L && l >= W.la && l < W.lb && first[q] < W.hi)
-                   ? (u32)((W.hi - first[q] - 1) / P.M + 1) : 0u;
+        const u32 r = (u32)rho[q];
+        b[q] = r < W.lomod ? 1u : 0u;
+        const u32 d = r + (b[q] ? (u32)P.M : 0u) - W.lomod;       // (rho - lo) mod M
+        n[q] = (l < P.L && l >= W.la && l < W.lb) ? W.lq + (d < W.lr ? 1u : 0u) : 0u;
         nmax = max(nmax, n[q]);
       }
       if (nmax == 0) continue;
+      #pragma unroll
+      for (int q = 0; q < SHORT_LANES; ++q) first[q] = rho[q] + P.M * (W.Q + b[q]);
       switch ((nmax + 31) >> 5) {
         case 1: short_segments<1>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
         case 2: short_segments<2>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
@@ -853,7 +855,8 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
           la = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod) - e->classes.begin();
           lb = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod + len) - e->classes.begin();
         }
-        if (la < lb) shortw.push_back(ShortWin{d.Q, d.hi, d.lomod, (u32)i, (u32)la, (u32)lb});
+        if (la < lb)
+          shortw.push_back(ShortWin{d.Q, d.lomod, (u32)i, (u32)la, (u32)lb, (u32)(len / M), (u32)(len % M)});
       }
     } else {
       d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG); d.groups = (u32)L;
@@ -1275,9 +1278,12 @@ static es_status probe(es_engine *e, size_t count, size_t in_bytes, const void *
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMalloc(&d_outs[i], std::max<size_t>(outs[i].second, 8)));
   CU(cudaMemcpy(d_in, in, in_bytes, cudaMemcpyHostToDevice));
   CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), e->stream));
+  CU(cudaEventRecord(e->ev[9], e->stream));
   launch(d_in, d_outs);
   CU(cudaGetLastError());
+  CU(cudaEventRecord(e->ev[10], e->stream));
   CU(cudaStreamSynchronize(e->stream));
+  e->timing.total_ms = ev_ms(e->ev[9], e->ev[10]);   // the probe kernel alone
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMemcpy(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost));
   u32 st = 0;
   CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
@@ -1347,7 +1353,7 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   e->sieve_p = cfg->sieve_p;
   e->device = cfg->device;
   e->flags = cfg->flags;
-  if (e->M < 2 || e->M > 0xFFFFFFFFull) { delete e; return ES_ERR_ARG; }
+  if (e->M < 2 || e->M > 0x7FFFFFFFull) { g_open_error = "wheel modulus must be below 2^31"; delete e; return ES_ERR_ARG; }
   const std::vector<Cover> covers = gen_covers(e->mmax);
   const Wheel w = build_wheel(e->M, gen_wheel_covers(e->M), gen_ucerts(UCERT_RMAX, UCERT_UMAX));
   e->classes = w.classes;

@@ -86,9 +86,11 @@ constexpr u32 MASK_BYTES_MAX = 48 * 1024;   // per-lane mask table budget (share
 struct MaskDesc { u32 s, d, off, c32; };    // stride, its index in sdist, 32-bit word offset, 32 mod s
 
 // A short window as k_mark_short walks it: lanes outside [la, lb) have no position in it.
+// Lane rho holds lq + [(rho - lo) mod M < lr] positions, lq = len / M, lr = len mod M (the
+// count of p == rho (mod M) in [lo, lo + len)).
 struct ShortWin {
-  u64 Q, hi;
-  u32 lomod, wi, la, lb;
+  u64 Q;
+  u32 lomod, wi, la, lb, lq, lr;
 };
 
 struct ShortParams {
