@@ -564,7 +564,7 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
 constexpr int RUNG_WARPS = 4;
 
 // Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung).
-__global__ void __launch_bounds__(RUNG_WARPS * 32) k_rung(const TailParams T, int no_rung) {
+__global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T, int no_rung) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -617,7 +617,7 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
     if (lane == 0) out[i] = pr ? 1 : 0;
   }
 }
-__global__ void __launch_bounds__(RUNG_WARPS * 32) k_probe_rung(const u64 *p, u64 count, RecDev *out,
+__global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
                                                                const TdEntry *tde, u32 *status) {
   __shared__ WarpFac F[RUNG_WARPS];

@@ -66,56 +66,78 @@ __device__ inline bool warp_is_prime(u64 n, u32 lane) {
   return __all_sync(FULL, ok);
 }
 
-// Brent's rho in every lane with its own constant; returns a nontrivial factor of the odd
-// composite n (the same value in every lane), or 0 when every lane exhausted its budget.
+// Brent's backtrack from ys: step one at a time until gcd(|x - ys|, n) > 1 (bounded).
+__device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const Mont &M) {
+  u64 g = 1;
+  for (u32 guard = 0; g == 1 && guard < 256; ++guard) {
+    ys = addmod(mmul(ys, ys, M), cm, n);
+    const u64 diff = x > ys ? x - ys : ys - x;
+    g = gcd64(diff ? diff : n, n);
+  }
+  return g;
+}
+
+// Brent's rho with two walks per lane (64 per warp, constants c = 1 + lane + 32j): the two
+// walks advance in lockstep through the same schedule (y -> y^2 + c in Montgomery form,
+// products of |x - y| batched 128 at a time between gcds, the cycle length doubling), so their
+// multiply chains interleave and the warp gets twice the walks for about the latency of one.
+// A walk whose batch product shares all of n backtracks one step at a time from the batch
+// start. Returns a nontrivial factor of the odd composite n (the same value in every lane),
+// or 0 when every lane exhausted its budget. The factorization is unique, so which walk wins
+// cannot change any result.
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
   if (lane == 0) *found = 0;
   __syncwarp();
   const Mont M = mont_init(n);
   u64 result = 0;
   u64 budget = WARP_RHO_STEPS;
-  for (u64 c = 1 + lane; c < 4096 && result == 0 && *found == 0 && budget; c += 32) {
-    const u64 cm = to_mont(c, M);
-    u64 y = to_mont(2, M), g = 1, r = 1, q = M.one, x = 0, ys = 0;
-    const u64 m = 128;
-    while (g == 1 && *found == 0) {
-      x = y;
+  const u64 m = 128;
+  for (u64 c1 = 1 + lane; c1 < 4096 && result == 0 && *found == 0 && budget; c1 += 64) {
+    const u64 c2 = c1 + 32;
+    const u64 cm1 = to_mont(c1, M), cm2 = to_mont(c2, M);
+    u64 y1 = to_mont(2, M), y2 = y1, q1 = M.one, q2 = M.one, x1 = 0, x2 = 0, ys1 = 0, ys2 = 0;
+    u64 g1 = 1, g2 = 1, r = 1;
+    while (g1 == 1 && g2 == 1 && *found == 0) {
+      x1 = y1;
+      x2 = y2;
       if (budget < r) { budget = 0; break; }
       budget -= r;
-      for (u64 i = 0; i < r; ++i) y = addmod(mmul(y, y, M), cm, n);
-      for (u64 k = 0; k < r && g == 1; k += m) {
-        ys = y;
+      for (u64 i = 0; i < r; ++i) {
+        y1 = addmod(mmul(y1, y1, M), cm1, n);
+        y2 = addmod(mmul(y2, y2, M), cm2, n);
+      }
+      for (u64 k = 0; k < r && g1 == 1 && g2 == 1; k += m) {
+        ys1 = y1;
+        ys2 = y2;
         const u64 lim = m < r - k ? m : r - k;
         if (budget < lim) { budget = 0; break; }
         budget -= lim;
         for (u64 i = 0; i < lim; ++i) {
-          y = addmod(mmul(y, y, M), cm, n);
-          if (y == x) { g = n; break; }
-          q = mmul(q, x > y ? x - y : y - x, M);
+          y1 = addmod(mmul(y1, y1, M), cm1, n);
+          y2 = addmod(mmul(y2, y2, M), cm2, n);
+          q1 = mmul(q1, x1 > y1 ? x1 - y1 : y1 - x1, M);   // a closed cycle makes q 0: gcd n
+          q2 = mmul(q2, x2 > y2 ? x2 - y2 : y2 - x2, M);
         }
-        if (g == n) break;
-        g = gcd64(q, n);
+        g1 = gcd64(q1, n);
+        g2 = gcd64(q2, n);
         if (*found) break;
       }
       r <<= 1;
       if (r > (1ull << 26) || budget == 0) break;
     }
-    if (g == n || (g == 1 && budget && *found == 0)) {
-      g = 1;
-      for (u64 guard = 0; g == 1 && guard < (1ull << 20); ++guard) {
-        ys = addmod(mmul(ys, ys, M), cm, n);
-        const u64 diff = x > ys ? x - ys : ys - x;
-        g = gcd64(diff ? diff : n, n);
-        if (ys == x) break;
-      }
+    if (g1 != 1 && g1 != n) result = g1;
+    else if (g2 != 1 && g2 != n) result = g2;
+    else {
+      if (g1 == n) { const u64 g = rho_backtrack(x1, ys1, cm1, n, M); if (g != 1 && g != n) result = g; }
+      if (!result && g2 == n) { const u64 g = rho_backtrack(x2, ys2, cm2, n, M); if (g != 1 && g != n) result = g; }
     }
-    if (g != 1 && g != n) { result = g; *found = g; }
+    if (result) *found = result;
   }
   __syncwarp();
   const unsigned has = __ballot_sync(FULL, result != 0);
   if (has) return __shfl_sync(FULL, result, __ffs(has) - 1);
   const u64 f = *found;
-  if (!f) atomicOr(status, ST_RHO_BUDGET);
+  if (!f && lane == 0) atomicOr(status, ST_RHO_BUDGET);
   return f;
 }
 
@@ -130,51 +152,60 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
   if (tz) { n >>= tz; wf_add(F, 2, tz, lane); }
   u64 cur = n;                 // n with every prime found so far divided out
   bool complete = true;        // every odd prime < 2^16 was tested
-  for (int c = 0; c < TD_CHUNKS; ++c) {
-    const int i = c * 32 + lane;
-    bool hit = false;
-    u64 f = 1;
-    int e = 0;
-    u32 d = 0;
-    if (i < NTD) {
-      d = __ldg(tdp + i);
-      const TdEntry t = tde[i];
-      u64 x = n * t.inv;
-      if (x <= t.lim) {
-        hit = true;
-        u64 m = x;
-        e = 1;
-        f = t.inv;
-        for (int g = 0; g < 64; ++g) {
-          x = m * t.inv;
-          if (x > t.lim) break;
-          m = x; ++e; f *= t.inv;
+  // Blocks of TD_UNROLL chunks: every table load of a block is issued before any test, so
+  // the block pays one load latency instead of one per chunk. Testing primes past the point
+  // where d^2 > cur is harmless (each prime is tested once, against n, and a hit is a genuine
+  // factor), so the early exit is checked once per block.
+  constexpr int TD_UNROLL = 8;
+  for (int cb = 0; cb < TD_CHUNKS; cb += TD_UNROLL) {
+    u64 inv[TD_UNROLL], lim[TD_UNROLL];
+    #pragma unroll
+    for (int j = 0; j < TD_UNROLL; ++j) {
+      const int i = (cb + j) * 32 + lane;
+      if (i < NTD) { const TdEntry t = tde[i]; inv[j] = t.inv; lim[j] = t.lim; }
+      else { inv[j] = 0; lim[j] = 0; }
+    }
+    const int nx = (cb + TD_UNROLL) * 32;
+    const u64 dn = nx < NTD ? (u64)__ldg(tdp + nx) : 0;
+    #pragma unroll
+    for (int j = 0; j < TD_UNROLL; ++j) {
+      const int i = (cb + j) * 32 + lane;
+      u64 x = n * inv[j];
+      const bool hit = i < NTD && x <= lim[j];
+      const unsigned mask = __ballot_sync(FULL, hit);
+      if (mask) {                                  // rare: a prime below 2^16 divides n
+        u64 f = 1;
+        int e = 0;
+        if (hit) {
+          u64 m = x;
+          e = 1;
+          f = inv[j];
+          for (int g = 0; g < 64; ++g) {
+            x = m * inv[j];
+            if (x > lim[j]) break;
+            m = x; ++e; f *= inv[j];
+          }
         }
+        const int base = F.k;
+        __syncwarp();
+        if (hit) {
+          const int pos = base + __popc(mask & ((1u << lane) - 1));
+          if (pos < MAXF) { F.pr[pos] = __ldg(tdp + i); F.ex[pos] = e; }
+        }
+        u64 g = f;
+        #pragma unroll
+        for (int o = 16; o; o >>= 1) g *= __shfl_xor_sync(FULL, g, o);
+        cur *= g;                                  // exact: divides out every d^e found
+        __syncwarp();
+        if (lane == 0) {
+          const int nk = base + __popc(mask);
+          if (nk > MAXF) F.overflow = 1;
+          F.k = nk > MAXF ? MAXF : nk;
+        }
+        __syncwarp();
       }
     }
-    const unsigned mask = __ballot_sync(FULL, hit);
-    if (mask) {
-      const int base = F.k;
-      __syncwarp();
-      if (hit) {
-        const int pos = base + __popc(mask & ((1u << lane) - 1));
-        if (pos < MAXF) { F.pr[pos] = d; F.ex[pos] = e; }
-      }
-      u64 g = f;
-      #pragma unroll
-      for (int o = 16; o; o >>= 1) g *= __shfl_xor_sync(FULL, g, o);
-      cur *= g;                                    // exact: divides out every d^e found
-      __syncwarp();
-      if (lane == 0) {
-        const int nk = base + __popc(mask);
-        if (nk > MAXF) F.overflow = 1;
-        F.k = nk > MAXF ? MAXF : nk;
-      }
-      __syncwarp();
-    }
-    const int nx = (c + 1) * 32;
     if (nx >= NTD) break;
-    const u64 dn = __ldg(tdp + nx);
     if (dn * dn > cur) { complete = false; break; }   // cur is 1 or prime
   }
   if (cur > 1) {
