@@ -69,7 +69,7 @@ __device__ inline bool warp_is_prime(u64 n, u32 lane) {
 // Brent's backtrack from ys: step one at a time until gcd(|x - ys|, n) > 1 (bounded).
 __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const Mont &M) {
   u64 g = 1;
-  for (u32 guard = 0; g == 1 && guard < 256; ++guard) {
+  for (u32 guard = 0; g == 1 && guard < 1024; ++guard) {
     ys = addmod(mmul(ys, ys, M), cm, n);
     const u64 diff = x > ys ? x - ys : ys - x;
     g = gcd64(diff ? diff : n, n);
@@ -91,12 +91,15 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
   const Mont M = mont_init(n);
   u64 result = 0;
   u64 budget = WARP_RHO_STEPS;
-  const u64 m = 128;
+  // Larger batches than the reference's 128 and a first cycle length of 128 instead of 1:
+  // every cofactor that reaches rho has all its primes above 2^16, so its cycles are long,
+  // and a gcd (a few thousand cycles of binary steps) is worth amortising over more steps.
+  const u64 m = 512;
   for (u64 c1 = 1 + lane; c1 < 4096 && result == 0 && *found == 0 && budget; c1 += 64) {
     const u64 c2 = c1 + 32;
     const u64 cm1 = to_mont(c1, M), cm2 = to_mont(c2, M);
     u64 y1 = to_mont(2, M), y2 = y1, q1 = M.one, q2 = M.one, x1 = 0, x2 = 0, ys1 = 0, ys2 = 0;
-    u64 g1 = 1, g2 = 1, r = 1;
+    u64 g1 = 1, g2 = 1, r = 128;
     while (g1 == 1 && g2 == 1 && *found == 0) {
       x1 = y1;
       x2 = y2;
@@ -118,8 +121,11 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
           q1 = mmul(q1, x1 > y1 ? x1 - y1 : y1 - x1, M);   // a closed cycle makes q 0: gcd n
           q2 = mmul(q2, x2 > y2 ? x2 - y2 : y2 - x2, M);
         }
-        g1 = gcd64(q1, n);
-        g2 = gcd64(q2, n);
+        // one gcd for both walks; split only when their product shares a factor with n
+        if (gcd64(mmul(q1, q2, M), n) != 1) {
+          g1 = gcd64(q1, n);
+          g2 = gcd64(q2, n);
+        }
         if (*found) break;
       }
       r <<= 1;
