@@ -66,10 +66,12 @@ __device__ inline bool warp_is_prime(u64 n, u32 lane) {
   return __all_sync(FULL, ok);
 }
 
-// Brent's backtrack from ys: step one at a time until gcd(|x - ys|, n) > 1 (bounded).
+// Brent's backtrack from ys: step one at a time until gcd(|x - ys|, n) > 1 (bounded by the
+// longest batch).
+constexpr u32 RHO_BATCH_MAX_BACKTRACK = 512;
 __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const Mont &M) {
   u64 g = 1;
-  for (u32 guard = 0; g == 1 && guard < 1024; ++guard) {
+  for (u32 guard = 0; g == 1 && guard <= RHO_BATCH_MAX_BACKTRACK; ++guard) {
     ys = addmod(mmul(ys, ys, M), cm, n);
     const u64 diff = x > ys ? x - ys : ys - x;
     g = gcd64(diff ? diff : n, n);
@@ -77,66 +79,80 @@ __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const
   return g;
 }
 
-// Brent's rho with two walks per lane (64 per warp, constants c = 1 + lane + 32j): the two
-// walks advance in lockstep through the same schedule (y -> y^2 + c in Montgomery form,
-// products of |x - y| batched 128 at a time between gcds, the cycle length doubling), so their
-// multiply chains interleave and the warp gets twice the walks for about the latency of one.
-// A walk whose batch product shares all of n backtracks one step at a time from the batch
-// start. Returns a nontrivial factor of the odd composite n (the same value in every lane),
-// or 0 when every lane exhausted its budget. The factorization is unique, so which walk wins
-// cannot change any result.
+// Brent's rho with RHO_WALKS walks per lane (constants c = 1 + lane + 32j): the walks of a
+// lane advance in lockstep through one schedule (y -> y^2 + c in Montgomery form, products of
+// |x - y| accumulated between gcds, the comparison window doubling), so their independent
+// multiply chains fill the issue slots that one chain leaves idle -- a lone walk is
+// latency-bound at ~0.4 instructions per cycle. One gcd per batch tests the product of all
+// the lane's accumulators; only a batch that shares a factor with n is split walk by walk.
+// A walk whose product shares all of n backtracks one step at a time from the batch start.
+// Returns a nontrivial factor of the odd composite n (the same value in every lane), or 0 when
+// every lane exhausted its budget. The factorization is unique, so which walk wins cannot
+// change any result.
+constexpr int RHO_WALKS = 4;
+constexpr u64 RHO_R0 = 16;      // first comparison window
+constexpr u64 RHO_BATCH = 256;  // steps between gcds
+
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
   if (lane == 0) *found = 0;
   __syncwarp();
   const Mont M = mont_init(n);
   u64 result = 0;
   u64 budget = WARP_RHO_STEPS;
-  // Larger batches than the reference's 128 and a first cycle length of 128 instead of 1:
-  // every cofactor that reaches rho has all its primes above 2^16, so its cycles are long,
-  // and a gcd (a few thousand cycles of binary steps) is worth amortising over more steps.
-  const u64 m = 512;
-  for (u64 c1 = 1 + lane; c1 < 4096 && result == 0 && *found == 0 && budget; c1 += 64) {
-    const u64 c2 = c1 + 32;
-    const u64 cm1 = to_mont(c1, M), cm2 = to_mont(c2, M);
-    u64 y1 = to_mont(2, M), y2 = y1, q1 = M.one, q2 = M.one, x1 = 0, x2 = 0, ys1 = 0, ys2 = 0;
-    u64 g1 = 1, g2 = 1, r = 128;
-    while (g1 == 1 && g2 == 1 && *found == 0) {
-      x1 = y1;
-      x2 = y2;
+  const u64 y0 = to_mont(2, M);
+  for (u64 cbase = 1 + lane; cbase < 4096 && result == 0 && *found == 0 && budget; cbase += 32 * RHO_WALKS) {
+    u64 cm[RHO_WALKS], y[RHO_WALKS], q[RHO_WALKS], x[RHO_WALKS], ys[RHO_WALKS], g[RHO_WALKS];
+    #pragma unroll
+    for (int w = 0; w < RHO_WALKS; ++w) {
+      cm[w] = to_mont(cbase + 32 * w, M);
+      y[w] = y0; q[w] = M.one; x[w] = 0; ys[w] = 0; g[w] = 1;
+    }
+    bool hit = false;
+    u64 r = RHO_R0;
+    while (!hit && *found == 0) {
+      #pragma unroll
+      for (int w = 0; w < RHO_WALKS; ++w) x[w] = y[w];
       if (budget < r) { budget = 0; break; }
       budget -= r;
       for (u64 i = 0; i < r; ++i) {
-        y1 = addmod(mmul(y1, y1, M), cm1, n);
-        y2 = addmod(mmul(y2, y2, M), cm2, n);
+        #pragma unroll
+        for (int w = 0; w < RHO_WALKS; ++w) y[w] = addmod(mmul(y[w], y[w], M), cm[w], n);
       }
-      for (u64 k = 0; k < r && g1 == 1 && g2 == 1; k += m) {
-        ys1 = y1;
-        ys2 = y2;
-        const u64 lim = m < r - k ? m : r - k;
+      for (u64 k = 0; k < r && !hit; k += RHO_BATCH) {
+        #pragma unroll
+        for (int w = 0; w < RHO_WALKS; ++w) ys[w] = y[w];
+        const u64 lim = RHO_BATCH < r - k ? RHO_BATCH : r - k;
         if (budget < lim) { budget = 0; break; }
         budget -= lim;
         for (u64 i = 0; i < lim; ++i) {
-          y1 = addmod(mmul(y1, y1, M), cm1, n);
-          y2 = addmod(mmul(y2, y2, M), cm2, n);
-          q1 = mmul(q1, x1 > y1 ? x1 - y1 : y1 - x1, M);   // a closed cycle makes q 0: gcd n
-          q2 = mmul(q2, x2 > y2 ? x2 - y2 : y2 - x2, M);
+          #pragma unroll
+          for (int w = 0; w < RHO_WALKS; ++w) {
+            y[w] = addmod(mmul(y[w], y[w], M), cm[w], n);
+            q[w] = mmul(q[w], x[w] > y[w] ? x[w] - y[w] : y[w] - x[w], M);   // a closed cycle makes q 0
+          }
         }
-        // one gcd for both walks; split only when their product shares a factor with n
-        if (gcd64(mmul(q1, q2, M), n) != 1) {
-          g1 = gcd64(q1, n);
-          g2 = gcd64(q2, n);
+        u64 all = q[0];
+        #pragma unroll
+        for (int w = 1; w < RHO_WALKS; ++w) all = mmul(all, q[w], M);
+        if (gcd64(all, n) != 1) {
+          hit = true;
+          #pragma unroll
+          for (int w = 0; w < RHO_WALKS; ++w) g[w] = gcd64(q[w], n);
         }
         if (*found) break;
       }
       r <<= 1;
       if (r > (1ull << 26) || budget == 0) break;
     }
-    if (g1 != 1 && g1 != n) result = g1;
-    else if (g2 != 1 && g2 != n) result = g2;
-    else {
-      if (g1 == n) { const u64 g = rho_backtrack(x1, ys1, cm1, n, M); if (g != 1 && g != n) result = g; }
-      if (!result && g2 == n) { const u64 g = rho_backtrack(x2, ys2, cm2, n, M); if (g != 1 && g != n) result = g; }
-    }
+    #pragma unroll
+    for (int w = 0; w < RHO_WALKS; ++w)
+      if (!result && g[w] != 1 && g[w] != n) result = g[w];
+    #pragma unroll
+    for (int w = 0; w < RHO_WALKS; ++w)
+      if (!result && g[w] == n) {
+        const u64 gb = rho_backtrack(x[w], ys[w], cm[w], n, M);
+        if (gb != 1 && gb != n) result = gb;
+      }
     if (result) *found = result;
   }
   __syncwarp();
