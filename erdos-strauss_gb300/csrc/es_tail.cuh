@@ -79,17 +79,20 @@ __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const
   return g;
 }
 
-// Brent's rho with RHO_WALKS walks per lane (constants c = 1 + lane + 32j): the walks of a
-// lane advance in lockstep through one schedule (y -> y^2 + c in Montgomery form, products of
-// |x - y| accumulated between gcds, the comparison window doubling), so their independent
-// multiply chains fill the issue slots that one chain leaves idle -- a lone walk is
-// latency-bound at ~0.4 instructions per cycle. One gcd per batch tests the product of all
-// the lane's accumulators; only a batch that shares a factor with n is split walk by walk.
-// A walk whose product shares all of n backtracks one step at a time from the batch start.
-// Returns a nontrivial factor of the odd composite n (the same value in every lane), or 0 when
-// every lane exhausted its budget. The factorization is unique, so which walk wins cannot
-// change any result.
-constexpr int RHO_WALKS = 4;
+// Brent's rho, one walk per lane (constants c = 1 + lane + 32j for successive tries): the
+// schedule of sieve/rung_scan3.cpp:333-369 -- y -> y^2 + c in Montgomery form, products of
+// |x - y| accumulated between gcds, the comparison window doubling -- with two changes that
+// cannot change a result, only when a factor is found: the first window is 16 steps instead
+// of 1 (every cofactor that reaches rho has all its primes above 2^16, so its cycles are far
+// longer) and gcds come every 256 steps instead of 128 (a 64-bit binary gcd costs about as
+// much as twenty steps here). A 64-bit Montgomery multiply is issue-bound on this GPU (the
+// wide integer multiplies issue at a quarter of the low-half rate), so more walks per lane
+// would only add work: the latency-optimal split is one walk per lane.
+// A walk whose batch product shares all of n backtracks one step at a time from the batch
+// start. Returns a nontrivial factor of the odd composite n (the same value in every lane),
+// or 0 when every lane exhausted its budget. The factorization is unique, so which walk wins
+// cannot change any result.
+constexpr int RHO_WALKS = 1;
 constexpr u64 RHO_R0 = 16;      // first comparison window
 constexpr u64 RHO_BATCH = 256;  // steps between gcds
 
@@ -134,10 +137,14 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
         u64 all = q[0];
         #pragma unroll
         for (int w = 1; w < RHO_WALKS; ++w) all = mmul(all, q[w], M);
-        if (gcd64(all, n) != 1) {
+        const u64 ga = gcd64(all, n);
+        if (ga != 1) {
           hit = true;
-          #pragma unroll
-          for (int w = 0; w < RHO_WALKS; ++w) g[w] = gcd64(q[w], n);
+          if (RHO_WALKS == 1) g[0] = ga;
+          else {
+            #pragma unroll
+            for (int w = 0; w < RHO_WALKS; ++w) g[w] = gcd64(q[w], n);
+          }
         }
         if (*found) break;
       }
