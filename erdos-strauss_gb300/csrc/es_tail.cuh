@@ -96,14 +96,23 @@ constexpr int RHO_WALKS = 1;
 constexpr u64 RHO_R0 = 16;      // first comparison window
 constexpr u64 RHO_BATCH = 256;  // steps between gcds
 
-__device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status) {
+// cancel/my_k: the warp is working for rung index my_k of a block whose best certifying rung
+// so far is *cancel; once that drops below my_k nothing this warp finds can matter and it stops
+// (returning 0 without an error). cancel may be null.
+__device__ __forceinline__ bool cancelled(const volatile int *cancel, int my_k) {
+  return cancel && *cancel < my_k;
+}
+
+__device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
+                               int my_k = 0) {
   if (lane == 0) *found = 0;
   __syncwarp();
   const Mont M = mont_init(n);
   u64 result = 0;
   u64 budget = WARP_RHO_STEPS;
   const u64 y0 = to_mont(2, M);
-  for (u64 cbase = 1 + lane; cbase < 4096 && result == 0 && *found == 0 && budget; cbase += 32 * RHO_WALKS) {
+  for (u64 cbase = 1 + lane; cbase < 4096 && result == 0 && *found == 0 && budget && !cancelled(cancel, my_k);
+       cbase += 32 * RHO_WALKS) {
     u64 cm[RHO_WALKS], y[RHO_WALKS], q[RHO_WALKS], x[RHO_WALKS], ys[RHO_WALKS], g[RHO_WALKS];
     #pragma unroll
     for (int w = 0; w < RHO_WALKS; ++w) {
@@ -112,7 +121,7 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
     }
     bool hit = false;
     u64 r = RHO_R0;
-    while (!hit && *found == 0) {
+    while (!hit && *found == 0 && !cancelled(cancel, my_k)) {
       #pragma unroll
       for (int w = 0; w < RHO_WALKS; ++w) x[w] = y[w];
       if (budget < r) { budget = 0; break; }
@@ -146,7 +155,7 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
             for (int w = 0; w < RHO_WALKS; ++w) g[w] = gcd64(q[w], n);
           }
         }
-        if (*found) break;
+        if (*found || cancelled(cancel, my_k)) break;
       }
       r <<= 1;
       if (r > (1ull << 26) || budget == 0) break;
@@ -166,14 +175,15 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
   const unsigned has = __ballot_sync(FULL, result != 0);
   if (has) return __shfl_sync(FULL, result, __ffs(has) - 1);
   const u64 f = *found;
-  if (!f && lane == 0) atomicOr(status, ST_RHO_BUDGET);
+  if (!f && lane == 0 && !cancelled(cancel, my_k)) atomicOr(status, ST_RHO_BUDGET);
   return f;
 }
 
 // Complete factorization of n >= 1 into F (prime order as found). All lanes call.
 // Returns false when a bound was hit (status says which).
 __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
-                            u32 *status, u32 lane, volatile u64 *rho_slot) {
+                                   u32 *status, u32 lane, volatile u64 *rho_slot,
+                                   const volatile int *cancel = nullptr, int my_k = 0) {
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
   if (n <= 1) return true;
@@ -252,8 +262,8 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
         const u64 s = isqrt64(v);
         if (s * s == v) { wf_add(F, s, 2, lane); continue; }
-        const u64 d = warp_rho(v, lane, rho_slot, status);
-        if (d == 0) return false;
+        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k);
+        if (d == 0) return false;                  // budget (status set) or cancelled
         if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
         stack[sp++] = d;
         stack[sp++] = v / d;
@@ -348,7 +358,7 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *td
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w)) break;
+    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k)) break;
     const U128 q{p * A, __umul64hi(p, A)};
     const U128 u = warp_min_div_res(p, F[w], q, r, target, D[w], lane);
     if (u.lo == 0 && u.hi == 0) continue;
