@@ -14,6 +14,8 @@ records and counters returned to the host.
           (window list in, counters and sorted binary records out)
   plain   the same windows through per-window launches of the same kernels
   c3      one 2^34-integer window at height >= 1.7e19, plain launch (the "at 1e19" row)
+  serve   2000 single-window requests arriving as a Poisson stream through es_submit/es_poll
+          (continuous batching over two streams): p50/p99 latency and integers/s
 
 --impl reference times the reference algorithm on the host cores (the CPU oracle port, all
 threads) on a bounded sample of the same workload. Multi-GPU: one process per GPU under
@@ -51,6 +53,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--serve", type=int, default=2000, help="serving requests (0: no serving leg)")
     return ap.parse_args()
 
 
@@ -213,6 +216,66 @@ def run_reference(args, ws, rank):
     print(json.dumps(line))
 
 
+def percentile(xs, q):
+    """Nearest-rank percentile of a non-empty list."""
+    ys = sorted(xs)
+    return ys[min(len(ys) - 1, max(0, int(-(-q * len(ys) // 100)) - 1))]
+
+
+def serve_leg(eng, n, seed):
+    """Serving: n requests arriving as a Poisson stream (mean gap 0.5 ms, lengths 2^12..2^30,
+    workloads.serve_requests) through es_submit / es_poll. A submitting thread keeps the arrival
+    times; the main thread sweeps the outstanding tickets without blocking. Latency = completion
+    seen by the sweep - scheduled arrival."""
+    import threading
+    import es_sieve
+    reqs = workloads.serve_requests(n, seed=seed)
+    tickets = [None] * n
+    refused = [0]
+    t0 = time.perf_counter() + 0.01
+
+    def submitter():
+        for i, (t, lo, hi) in enumerate(reqs):
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            while True:
+                try:
+                    tickets[i] = eng.submit([(lo, hi)])
+                    break
+                except es_sieve.EsError as ex:
+                    if ex.status != es_sieve.ES_ERR_BUSY:
+                        raise
+                    refused[0] += 1
+                    time.sleep(0.0005)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    done_at = [None] * n
+    left = set(range(n))
+    while left:
+        for i in sorted(left):
+            if tickets[i] is None:
+                break
+            try:
+                eng.poll(tickets[i], 1, timeout_ms=0)
+            except es_sieve.EsError as ex:
+                if ex.status != es_sieve.ES_ERR_TIMEOUT:
+                    raise
+                continue
+            done_at[i] = time.perf_counter()
+            left.discard(i)
+        time.sleep(0.00005)
+    th.join()
+    lat = [1000.0 * (done_at[i] - (t0 + reqs[i][0])) for i in range(n)]
+    span = max(done_at) - (t0 + reqs[0][0])
+    ints = sum(hi - lo for _, lo, hi in reqs)
+    return {"requests": n, "arrivals": "poisson, mean gap 0.5 ms, lengths 2^12..2^30 log-uniform",
+            "offered_integers_per_s": ints / reqs[-1][0], "integers_per_s": ints / span,
+            "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99), "max_ms": max(lat),
+            "busy_refusals": refused[0]}
+
+
 def run_gpu(args, ws, rank, local):
     import es_sieve
     flush, flush_note = l2_flusher(local)
@@ -266,6 +329,9 @@ def run_gpu(args, ws, rank, local):
         t3 = eng.timing()
         extra["c3"] = {"value": (c3["hi"] - c3["lo"]) / (t3["total_ms"] / 1000.0), "ms_per_step": t3["total_ms"],
                        "lo": c3["lo"], "mark_ms": t3["mark_ms"], "rung_ms": t3["rung_ms"]}
+    if args.serve:
+        serve_leg(eng, min(200, args.serve), workloads.SEED + 7)          # warm the serving slots
+        extra["serve"] = serve_leg(eng, args.serve, workloads.SEED + 1000 * (rank + 1))
     # roofline of the dominant kernel (per-kernel CUDA events on the engine's stream)
     hbm, peak_kind = peaks()
     per_kernel = {"k_mark_short": kern["mark_short_ms"], "k_mark": kern["mark_long_ms"], "k_prep": kern["prep_ms"],

@@ -679,6 +679,52 @@ constexpr int SHORT_BLOCK = 256;
 
 }  // namespace es
 
+namespace es {
+// Everything one run needs besides the resident tables: a stream, its events, the per-run
+// device buffers and their pinned host staging, and the captured graph. An engine has one
+// slot for its synchronous calls and SERVE_SLOTS more for the serving workers, so that
+// several batches can be in flight on their own streams.
+struct Slot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[12] = {};
+  BatchHdr *d_hdr = nullptr, *h_hdr = nullptr;
+  WinDev *h_win = nullptr;
+  ShortWin *h_short = nullptr;
+  WinCount *h_cnt = nullptr;
+  unsigned long long *h_ctr = nullptr;
+  u32 *h_status = nullptr;
+  RecDev *h_recs = nullptr;
+  cudaGraph_t graph = nullptr;          // the persistent schedule, captured once per capacity
+  cudaGraphExec_t gexec = nullptr;
+  WinDev *d_win = nullptr; size_t win_cap = 0;
+  WinCount *d_cnt = nullptr;
+  ShortWin *d_shortw = nullptr; size_t shortw_cap = 0;
+  u16 *d_Qm = nullptr; size_t qm_cap = 0;
+  Surv *d_surv = nullptr;
+  u32 *d_primes = nullptr, *d_direct = nullptr, *d_cand = nullptr;
+  RecDev *d_recs = nullptr;
+  size_t cap = 0;
+  unsigned long long *d_ctr = nullptr;  // [0] queue [1] surv [2] prime [3] direct [4] rec [5] cand
+  u32 *d_status = nullptr;
+  es_timing_t timing{};
+  std::mutex mu;                        // one run at a time per slot
+};
+
+constexpr int SERVE_SLOTS = 2;
+
+// A serving request: windows in, counters and records out.
+struct Request {
+  uint64_t ticket = 0;
+  std::vector<es_window> w;
+  std::vector<es_counters> cnt;
+  std::vector<es_record> recs;
+  es_status st = ES_OK;
+  std::string err;
+  bool done = false;
+  u64 mem = 0;                          // admitted device-memory estimate
+};
+}  // namespace es
+
 struct es_engine {
   // configuration and derived tables
   es::u64 M = 0, mmax = 0, sieve_p = 0;
@@ -692,48 +738,36 @@ struct es_engine {
   std::vector<uint32_t> order;
   uint32_t nf = 0, ldk = 0, D = 0, Lpad = 0;
   int device = 0, sm_count = 0, mark_occupancy = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[12] = {};
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
   es::u16 *d_K0 = nullptr, *d_K0T = nullptr;
-  es::u16 *d_Qm = nullptr; size_t qm_cap = 0;
   // short-window kill masks
   es::u64 *d_mtab = nullptr;
   es::MaskDesc *d_mdesc = nullptr;
   es::u32 *d_lfil = nullptr;
-  es::ShortWin *d_shortw = nullptr;
-  size_t shortw_cap = 0;
   uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0;
   es::TdEntry *d_tde = nullptr;
-  // per-run buffers (device) and their pinned host staging
-  es::BatchHdr *d_hdr = nullptr, *h_hdr = nullptr;
-  es::WinDev *h_win = nullptr;
-  es::ShortWin *h_short = nullptr;
-  es::WinCount *h_cnt = nullptr;
-  unsigned long long *h_ctr = nullptr;
-  es::u32 *h_status = nullptr;
-  es::RecDev *h_recs = nullptr;
-  // the persistent schedule's launch sequence, captured once per buffer capacity
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  es::WinDev *d_win = nullptr; size_t win_cap = 0;
-  es::WinCount *d_cnt = nullptr;
-  es::Surv *d_surv = nullptr;
-  es::u32 *d_primes = nullptr, *d_direct = nullptr, *d_cand = nullptr;
-  es::RecDev *d_recs = nullptr;
-  size_t cap = 0;
-  unsigned long long *d_ctr = nullptr;   // [0] queue [1] surv [2] prime [3] direct [4] rec
-  es::u32 *d_status = nullptr;
-  es_timing_t timing{};
+  // slot 0: es_run_window / es_run_batch / probes; slots 1..SERVE_SLOTS: serving workers
+  es::Slot slots[1 + es::SERVE_SLOTS];
   std::string last_error;
-  std::mutex mu;                         // serialises device work on this engine
+  std::mutex err_mu;
+  // serving
+  size_t mem_budget = 0;
+  std::mutex qmu;
+  std::condition_variable qcv, dcv;
+  std::deque<es::Request *> queue;
+  std::map<uint64_t, es::Request *> reqs;
+  uint64_t next_ticket = 1;
+  es::u64 mem_in_use = 0;
+  size_t queued_windows = 0;
+  std::vector<std::thread> workers;
+  bool stopping = false;
 };
 
 namespace es {
 
 static es_status fail(es_engine *e, es_status s, const std::string &msg) {
-  if (e) e->last_error = msg;
+  if (e) { std::lock_guard<std::mutex> lk(e->err_mu); e->last_error = msg; }
   return s;
 }
 
@@ -744,78 +778,78 @@ static es_status fail(es_engine *e, es_status s, const std::string &msg) {
       return fail(e, ES_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));   \
   } while (0)
 
-static void drop_graph(es_engine *e) {
-  if (e->gexec) cudaGraphExecDestroy(e->gexec);
-  if (e->graph) cudaGraphDestroy(e->graph);
-  e->gexec = nullptr;
-  e->graph = nullptr;
+static void drop_graph(Slot *sl) {
+  if (sl->gexec) cudaGraphExecDestroy(sl->gexec);
+  if (sl->graph) cudaGraphDestroy(sl->graph);
+  sl->gexec = nullptr;
+  sl->graph = nullptr;
 }
 
 // Device buffers for nwin windows and a survivor capacity of cap, with their pinned host
 // staging. Growing any of them invalidates the captured graph (its copies and kernel
 // parameters name the old buffers and sizes).
-static es_status ensure_capacity(es_engine *e, size_t nwin, size_t cap) {
-  if (!e->d_hdr) {
-    CU(cudaMalloc(&e->d_hdr, sizeof(BatchHdr)));
-    CU(cudaMallocHost(&e->h_hdr, sizeof(BatchHdr)));
-    CU(cudaMallocHost(&e->h_ctr, 8 * sizeof(unsigned long long)));
-    CU(cudaMallocHost(&e->h_status, sizeof(u32)));
+static es_status ensure_capacity(es_engine *e, Slot *sl, size_t nwin, size_t cap) {
+  if (!sl->d_hdr) {
+    CU(cudaMalloc(&sl->d_hdr, sizeof(BatchHdr)));
+    CU(cudaMallocHost(&sl->h_hdr, sizeof(BatchHdr)));
+    CU(cudaMallocHost(&sl->h_ctr, 8 * sizeof(unsigned long long)));
+    CU(cudaMallocHost(&sl->h_status, sizeof(u32)));
   }
-  if (nwin > e->win_cap) {
-    drop_graph(e);
-    cudaFree(e->d_win); cudaFree(e->d_cnt); cudaFree(e->d_shortw); cudaFree(e->d_Qm);
-    cudaFreeHost(e->h_win); cudaFreeHost(e->h_short); cudaFreeHost(e->h_cnt);
-    e->d_win = nullptr; e->d_cnt = nullptr; e->d_shortw = nullptr; e->d_Qm = nullptr;
-    e->h_win = nullptr; e->h_short = nullptr; e->h_cnt = nullptr;
+  if (nwin > sl->win_cap) {
+    drop_graph(sl);
+    cudaFree(sl->d_win); cudaFree(sl->d_cnt); cudaFree(sl->d_shortw); cudaFree(sl->d_Qm);
+    cudaFreeHost(sl->h_win); cudaFreeHost(sl->h_short); cudaFreeHost(sl->h_cnt);
+    sl->d_win = nullptr; sl->d_cnt = nullptr; sl->d_shortw = nullptr; sl->d_Qm = nullptr;
+    sl->h_win = nullptr; sl->h_short = nullptr; sl->h_cnt = nullptr;
     const size_t want = std::max<size_t>(nwin, 64);
-    CU(cudaMalloc(&e->d_win, want * sizeof(WinDev)));
-    CU(cudaMalloc(&e->d_cnt, want * sizeof(WinCount)));
-    CU(cudaMalloc(&e->d_shortw, want * sizeof(ShortWin)));
-    CU(cudaMalloc(&e->d_Qm, want * std::max<u32>(e->D, 1) * sizeof(u16)));
-    CU(cudaMallocHost(&e->h_win, want * sizeof(WinDev)));
-    CU(cudaMallocHost(&e->h_short, want * sizeof(ShortWin)));
-    CU(cudaMallocHost(&e->h_cnt, want * sizeof(WinCount)));
-    e->win_cap = e->shortw_cap = want;
-    e->qm_cap = want * std::max<u32>(e->D, 1);
+    CU(cudaMalloc(&sl->d_win, want * sizeof(WinDev)));
+    CU(cudaMalloc(&sl->d_cnt, want * sizeof(WinCount)));
+    CU(cudaMalloc(&sl->d_shortw, want * sizeof(ShortWin)));
+    CU(cudaMalloc(&sl->d_Qm, want * std::max<u32>(e->D, 1) * sizeof(u16)));
+    CU(cudaMallocHost(&sl->h_win, want * sizeof(WinDev)));
+    CU(cudaMallocHost(&sl->h_short, want * sizeof(ShortWin)));
+    CU(cudaMallocHost(&sl->h_cnt, want * sizeof(WinCount)));
+    sl->win_cap = sl->shortw_cap = want;
+    sl->qm_cap = want * std::max<u32>(e->D, 1);
   }
-  if (cap > e->cap) {
-    drop_graph(e);
-    cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
-    cudaFreeHost(e->h_recs);
-    e->d_surv = nullptr; e->d_primes = e->d_direct = e->d_cand = nullptr; e->d_recs = nullptr; e->h_recs = nullptr;
-    CU(cudaMalloc(&e->d_surv, cap * sizeof(Surv)));
-    CU(cudaMalloc(&e->d_primes, cap * sizeof(u32)));
-    CU(cudaMalloc(&e->d_direct, cap * sizeof(u32)));
-    CU(cudaMalloc(&e->d_cand, cap * sizeof(u32)));
-    CU(cudaMalloc(&e->d_recs, cap * sizeof(RecDev)));
-    CU(cudaMallocHost(&e->h_recs, cap * sizeof(RecDev)));
-    e->cap = cap;
+  if (cap > sl->cap) {
+    drop_graph(sl);
+    cudaFree(sl->d_surv); cudaFree(sl->d_primes); cudaFree(sl->d_direct); cudaFree(sl->d_recs); cudaFree(sl->d_cand);
+    cudaFreeHost(sl->h_recs);
+    sl->d_surv = nullptr; sl->d_primes = sl->d_direct = sl->d_cand = nullptr; sl->d_recs = nullptr; sl->h_recs = nullptr;
+    CU(cudaMalloc(&sl->d_surv, cap * sizeof(Surv)));
+    CU(cudaMalloc(&sl->d_primes, cap * sizeof(u32)));
+    CU(cudaMalloc(&sl->d_direct, cap * sizeof(u32)));
+    CU(cudaMalloc(&sl->d_cand, cap * sizeof(u32)));
+    CU(cudaMalloc(&sl->d_recs, cap * sizeof(RecDev)));
+    CU(cudaMallocHost(&sl->h_recs, cap * sizeof(RecDev)));
+    sl->cap = cap;
   }
   return ES_OK;
 }
 
-static MarkParams mark_params(const es_engine *e) {
+static MarkParams mark_params(const es_engine *e, const Slot *sl) {
   MarkParams P;
   P.rho = e->d_rho; P.K0 = e->d_K0; P.K0T = e->d_K0T; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
-  P.Qm = e->d_Qm; P.Lpad = e->Lpad;
-  P.win = e->d_win; P.queue = reinterpret_cast<u64 *>(e->d_ctr + 0);
-  P.surv = e->d_surv; P.surv_count = e->d_ctr + 1; P.cnt = e->d_cnt;
-  P.hdr = e->d_hdr; P.surv_cap = e->cap; P.M = e->M;
+  P.Qm = sl->d_Qm; P.Lpad = e->Lpad;
+  P.win = sl->d_win; P.queue = reinterpret_cast<u64 *>(sl->d_ctr + 0);
+  P.surv = sl->d_surv; P.surv_count = sl->d_ctr + 1; P.cnt = sl->d_cnt;
+  P.hdr = sl->d_hdr; P.surv_cap = sl->cap; P.M = e->M;
   P.L = (u32)e->classes.size(); P.ldk = e->ldk; P.nf = e->nf; P.ncov = (u32)e->ncov;
   P.D = e->D;
   P.r_bytes = (4 * e->D + 15) & ~15u;
   return P;
 }
 
-static TailParams tail_params(const es_engine *e) {
+static TailParams tail_params(const es_engine *e, const Slot *sl) {
   TailParams T;
-  T.surv = e->d_surv; T.surv_count = e->d_ctr + 1;
-  T.cand = e->d_cand; T.cand_count = e->d_ctr + 5;
-  T.primes = e->d_primes; T.prime_count = e->d_ctr + 2;
-  T.direct = e->d_direct; T.direct_count = e->d_ctr + 3;
-  T.recs = e->d_recs; T.rec_count = e->d_ctr + 4;
-  T.cnt = e->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = e->d_status;
-  T.cap = e->cap;
+  T.surv = sl->d_surv; T.surv_count = sl->d_ctr + 1;
+  T.cand = sl->d_cand; T.cand_count = sl->d_ctr + 5;
+  T.primes = sl->d_primes; T.prime_count = sl->d_ctr + 2;
+  T.direct = sl->d_direct; T.direct_count = sl->d_ctr + 3;
+  T.recs = sl->d_recs; T.rec_count = sl->d_ctr + 4;
+  T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;
+  T.cap = sl->cap;
   return T;
 }
 
@@ -881,31 +915,31 @@ static u64 positions_in(const es_engine *e, u64 lo, u64 hi) {
 // tail, and the copies of the run counters back to pinned memory. With `capture` the event
 // records are external graph nodes, so that the kernels can still be timed when the
 // sequence runs as a graph. `items_hint` sizes k_mark's grid for the plain schedule.
-static es_status enqueue_funnel(es_engine *e, bool persistent, WinCount *cnt, size_t ncopy, size_t nshort_copy,
+static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCount *cnt, size_t ncopy, size_t nshort_copy,
                                 u64 items_hint, bool capture) {
-  MarkParams P = mark_params(e);
-  TailParams T = tail_params(e);
+  MarkParams P = mark_params(e, sl);
+  TailParams T = tail_params(e, sl);
   P.cnt = cnt;
   T.cnt = cnt;
-  cudaStream_t st = e->stream;
+  cudaStream_t st = sl->stream;
   auto rec = [&](int k) {
-    return capture ? cudaEventRecordWithFlags(e->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(e->ev[k], st);
+    return capture ? cudaEventRecordWithFlags(sl->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(sl->ev[k], st);
   };
-  CU(cudaMemsetAsync(e->d_ctr, 0, 8 * sizeof(unsigned long long), st));
-  CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), st));
-  CU(cudaMemcpyAsync(e->d_hdr, e->h_hdr, sizeof(BatchHdr), cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(e->d_win, e->h_win, ncopy * sizeof(WinDev), cudaMemcpyHostToDevice, st));
-  if (nshort_copy) CU(cudaMemcpyAsync(e->d_shortw, e->h_short, nshort_copy * sizeof(ShortWin), cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(sl->d_ctr, 0, 8 * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(sl->d_status, 0, sizeof(u32), st));
+  CU(cudaMemcpyAsync(sl->d_hdr, sl->h_hdr, sizeof(BatchHdr), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(sl->d_win, sl->h_win, ncopy * sizeof(WinDev), cudaMemcpyHostToDevice, st));
+  if (nshort_copy) CU(cudaMemcpyAsync(sl->d_shortw, sl->h_short, nshort_copy * sizeof(ShortWin), cudaMemcpyHostToDevice, st));
   CU(rec(0));
-  k_prep<<<e->sm_count * 4, 256, 0, st>>>(e->d_hdr, e->d_win, e->d_sdist, e->D, e->d_Qm);
+  k_prep<<<e->sm_count * 4, 256, 0, st>>>(sl->d_hdr, sl->d_win, e->d_sdist, e->D, sl->d_Qm);
   CU(cudaGetLastError());
   CU(rec(7));
   {
     ShortParams S;
-    S.rho = e->d_rho; S.K0 = e->d_K0; S.fdesc = e->d_fdesc; S.Qm = e->d_Qm; S.mtab = e->d_mtab;
-    S.mdesc = e->d_mdesc; S.lfil = e->d_lfil; S.win = e->d_win; S.shortw = e->d_shortw;
-    S.surv = e->d_surv; S.surv_count = e->d_ctr + 1; S.cnt = cnt; S.surv_cap = e->cap; S.M = e->M;
-    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad; S.hdr = e->d_hdr;
+    S.rho = e->d_rho; S.K0 = e->d_K0; S.fdesc = e->d_fdesc; S.Qm = sl->d_Qm; S.mtab = e->d_mtab;
+    S.mdesc = e->d_mdesc; S.lfil = e->d_lfil; S.win = sl->d_win; S.shortw = sl->d_shortw;
+    S.surv = sl->d_surv; S.surv_count = sl->d_ctr + 1; S.cnt = cnt; S.surv_cap = sl->cap; S.M = e->M;
+    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad; S.hdr = sl->d_hdr;
     S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all;
     k_mark_short<SHORT_BLOCK><<<(S.L + SHORT_LANES - 1) / SHORT_LANES, SHORT_BLOCK, short_smem(e), st>>>(S);
     CU(cudaGetLastError());
@@ -927,31 +961,31 @@ static es_status enqueue_funnel(es_engine *e, bool persistent, WinCount *cnt, si
   k_direct<<<e->sm_count, 32, 0, st>>>(T);
   CU(cudaGetLastError());
   CU(rec(4));
-  CU(cudaMemcpyAsync(e->h_ctr, e->d_ctr, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  CU(cudaMemcpyAsync(e->h_status, e->d_status, sizeof(u32), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(sl->h_ctr, sl->d_ctr, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(sl->h_status, sl->d_status, sizeof(u32), cudaMemcpyDeviceToHost, st));
   return ES_OK;
 }
 
 // The persistent schedule as a CUDA graph: counters cleared, the whole staging area copied,
 // every kernel, and the counters copied back, captured once and replayed per batch.
-static es_status capture_graph(es_engine *e) {
-  drop_graph(e);
-  CU(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+static es_status capture_graph(es_engine *e, Slot *sl) {
+  drop_graph(sl);
+  CU(cudaStreamBeginCapture(sl->stream, cudaStreamCaptureModeThreadLocal));
   es_status s = ES_OK;
-  const cudaError_t m = cudaMemsetAsync(e->d_cnt, 0, e->win_cap * sizeof(WinCount), e->stream);
-  if (m == cudaSuccess) s = enqueue_funnel(e, true, e->d_cnt, e->win_cap, e->shortw_cap, 0, true);
+  const cudaError_t m = cudaMemsetAsync(sl->d_cnt, 0, sl->win_cap * sizeof(WinCount), sl->stream);
+  if (m == cudaSuccess) s = enqueue_funnel(e, sl, true, sl->d_cnt, sl->win_cap, sl->shortw_cap, 0, true);
   if (m == cudaSuccess && s == ES_OK) {
-    const cudaError_t c2 = cudaMemcpyAsync(e->h_cnt, e->d_cnt, e->win_cap * sizeof(WinCount),
-                                           cudaMemcpyDeviceToHost, e->stream);
+    const cudaError_t c2 = cudaMemcpyAsync(sl->h_cnt, sl->d_cnt, sl->win_cap * sizeof(WinCount),
+                                           cudaMemcpyDeviceToHost, sl->stream);
     if (c2 != cudaSuccess) s = fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(c2));
   }
   cudaGraph_t g = nullptr;
-  const cudaError_t end = cudaStreamEndCapture(e->stream, &g);
+  const cudaError_t end = cudaStreamEndCapture(sl->stream, &g);
   if (m != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(m));
   if (s != ES_OK) { if (g) cudaGraphDestroy(g); return s; }
   if (end != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(end));
-  e->graph = g;
-  CU(cudaGraphInstantiate(&e->gexec, g, 0));
+  sl->graph = g;
+  CU(cudaGraphInstantiate(&sl->gexec, g, 0));
   return ES_OK;
 }
 
@@ -973,7 +1007,7 @@ static std::string status_text(u32 st) {
 
 // Runs windows through the funnel and collects counters and sorted records. Re-runs
 // with larger buffers when the survivor list overflowed (the count is exact even then).
-static es_status run_windows(es_engine *e, const es_window *w, size_t n, int schedule,
+static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
                              es_counters *per_window, es_records *recs) {
   const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
   for (size_t i = 0; i < n; ++i) {
@@ -988,92 +1022,92 @@ static es_status run_windows(es_engine *e, const es_window *w, size_t n, int sch
   u64 positions_bound = 0;
   for (size_t i = 0; i < n; ++i) positions_bound += positions_in(e, w[i].lo, w[i].hi);
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
-  cap = std::max(cap, e->cap);
+  cap = std::max(cap, sl->cap);
   const bool persistent = schedule == ES_SCHED_PERSISTENT;
   std::vector<RecDev> hr;
   bool done = false;
   for (int attempt = 0; attempt < 4 && !done; ++attempt) {
-    es_status s = ensure_capacity(e, n, cap);
+    es_status s = ensure_capacity(e, sl, n, cap);
     if (s) return s;
     double mark_ms = 0, mr_ms = 0, rung_ms = 0, direct_ms = 0, prep_ms = 0, short_ms = 0, long_ms = 0;
     u64 launches = 0, surv_max = 0, surv_total = 0, prime_total = 0;
     u32 status = 0;
     hr.clear();
     auto collect = [&]() -> es_status {   // after a pass: timings, counts, records
-      prep_ms += ev_ms(e->ev[0], e->ev[7]); short_ms += ev_ms(e->ev[7], e->ev[8]);
-      long_ms += ev_ms(e->ev[8], e->ev[1]);
-      mark_ms += ev_ms(e->ev[0], e->ev[1]); mr_ms += ev_ms(e->ev[1], e->ev[2]);
-      rung_ms += ev_ms(e->ev[2], e->ev[3]); direct_ms += ev_ms(e->ev[3], e->ev[4]);
-      const unsigned long long *ctr = e->h_ctr;
+      prep_ms += ev_ms(sl->ev[0], sl->ev[7]); short_ms += ev_ms(sl->ev[7], sl->ev[8]);
+      long_ms += ev_ms(sl->ev[8], sl->ev[1]);
+      mark_ms += ev_ms(sl->ev[0], sl->ev[1]); mr_ms += ev_ms(sl->ev[1], sl->ev[2]);
+      rung_ms += ev_ms(sl->ev[2], sl->ev[3]); direct_ms += ev_ms(sl->ev[3], sl->ev[4]);
+      const unsigned long long *ctr = sl->h_ctr;
       surv_max = std::max<u64>(surv_max, ctr[1]);
       surv_total += ctr[1]; prime_total += ctr[2];
-      status |= *e->h_status;
-      if (ctr[1] > e->cap) return ES_OK;
-      const size_t nrec = (size_t)std::min<u64>(ctr[4], e->cap);
+      status |= *sl->h_status;
+      if (ctr[1] > sl->cap) return ES_OK;
+      const size_t nrec = (size_t)std::min<u64>(ctr[4], sl->cap);
       if (nrec) {
-        CU(cudaMemcpyAsync(e->h_recs, e->d_recs, nrec * sizeof(RecDev), cudaMemcpyDeviceToHost, e->stream));
-        CU(cudaStreamSynchronize(e->stream));
-        hr.insert(hr.end(), e->h_recs, e->h_recs + nrec);
+        CU(cudaMemcpyAsync(sl->h_recs, sl->d_recs, nrec * sizeof(RecDev), cudaMemcpyDeviceToHost, sl->stream));
+        CU(cudaStreamSynchronize(sl->stream));
+        hr.insert(hr.end(), sl->h_recs, sl->h_recs + nrec);
       }
       return ES_OK;
     };
     if (persistent) {
-      e->h_hdr->total_items = total_items;
-      e->h_hdr->nwin = (u32)n;
-      e->h_hdr->nshort = (u32)shortw.size();
-      memcpy(e->h_win, wd.data(), n * sizeof(WinDev));
-      if (!shortw.empty()) memcpy(e->h_short, shortw.data(), shortw.size() * sizeof(ShortWin));
-      if (!e->gexec) { s = capture_graph(e); if (s) return s; }
-      CU(cudaGraphLaunch(e->gexec, e->stream));
-      CU(cudaStreamSynchronize(e->stream));
+      sl->h_hdr->total_items = total_items;
+      sl->h_hdr->nwin = (u32)n;
+      sl->h_hdr->nshort = (u32)shortw.size();
+      memcpy(sl->h_win, wd.data(), n * sizeof(WinDev));
+      if (!shortw.empty()) memcpy(sl->h_short, shortw.data(), shortw.size() * sizeof(ShortWin));
+      if (!sl->gexec) { s = capture_graph(e, sl); if (s) return s; }
+      CU(cudaGraphLaunch(sl->gexec, sl->stream));
+      CU(cudaStreamSynchronize(sl->stream));
       launches = 7;
       s = collect();
       if (s) return s;
     } else {
       // The plain schedule: the same kernels, one launch sequence per window.
-      CU(cudaMemsetAsync(e->d_cnt, 0, n * sizeof(WinCount), e->stream));
+      CU(cudaMemsetAsync(sl->d_cnt, 0, n * sizeof(WinCount), sl->stream));
       size_t k = 0;                      // next short-window entry (describe emits them in order)
       for (size_t i = 0; i < n; ++i) {
-        e->h_win[0] = wd[i];
-        e->h_win[0].item0 = 0;
+        sl->h_win[0] = wd[i];
+        sl->h_win[0].item0 = 0;
         const u64 items = (u64)wd[i].nseg * wd[i].groups;
         u32 nshort = 0;
-        if (k < shortw.size() && shortw[k].wi == i) { e->h_short[0] = shortw[k++]; e->h_short[0].wi = 0; nshort = 1; }
-        e->h_hdr->total_items = items; e->h_hdr->nwin = 1; e->h_hdr->nshort = nshort;
-        s = enqueue_funnel(e, false, e->d_cnt + i, 1, nshort, items, false);
+        if (k < shortw.size() && shortw[k].wi == i) { sl->h_short[0] = shortw[k++]; sl->h_short[0].wi = 0; nshort = 1; }
+        sl->h_hdr->total_items = items; sl->h_hdr->nwin = 1; sl->h_hdr->nshort = nshort;
+        s = enqueue_funnel(e, sl, false, sl->d_cnt + i, 1, nshort, items, false);
         if (s) return s;
-        CU(cudaStreamSynchronize(e->stream));
+        CU(cudaStreamSynchronize(sl->stream));
         launches += 7;
         const size_t base = hr.size();
         s = collect();
         if (s) return s;
-        if (surv_max > e->cap) break;
+        if (surv_max > sl->cap) break;
         for (size_t r = base; r < hr.size(); ++r) hr[r].win = (u32)i;
       }
-      CU(cudaMemcpyAsync(e->h_cnt, e->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost, e->stream));
-      CU(cudaStreamSynchronize(e->stream));
+      CU(cudaMemcpyAsync(sl->h_cnt, sl->d_cnt, n * sizeof(WinCount), cudaMemcpyDeviceToHost, sl->stream));
+      CU(cudaStreamSynchronize(sl->stream));
     }
-    if (surv_max > e->cap) {            // overflow: grow to the exact need and re-run
+    if (surv_max > sl->cap) {            // overflow: grow to the exact need and re-run
       cap = (size_t)(surv_max + surv_max / 4 + 1024);
       continue;
     }
     if (status) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(status));
-    e->timing.total_ms = mark_ms + mr_ms + rung_ms + direct_ms;   // kernels only, inputs resident
-    e->timing.mark_ms = mark_ms; e->timing.mr_ms = mr_ms;
-    e->timing.prep_ms = prep_ms; e->timing.mark_short_ms = short_ms; e->timing.mark_long_ms = long_ms;
-    e->timing.short_pairs = (u64)shortw.size() * e->classes.size();
-    e->timing.mask_bytes = shortw.empty() ? 0 : (u64)e->classes.size() * e->Wpad * 8;
-    e->timing.rung_ms = rung_ms; e->timing.direct_ms = direct_ms;
-    e->timing.marks_kernel_launches = persistent ? 1 : n;
-    e->timing.kernel_launches = launches;
-    e->timing.mark_items = total_items;
-    e->timing.survivors = surv_total;
-    e->timing.primes = prime_total;
+    sl->timing.total_ms = mark_ms + mr_ms + rung_ms + direct_ms;   // kernels only, inputs resident
+    sl->timing.mark_ms = mark_ms; sl->timing.mr_ms = mr_ms;
+    sl->timing.prep_ms = prep_ms; sl->timing.mark_short_ms = short_ms; sl->timing.mark_long_ms = long_ms;
+    sl->timing.short_pairs = (u64)shortw.size() * e->classes.size();
+    sl->timing.mask_bytes = shortw.empty() ? 0 : (u64)e->classes.size() * e->Wpad * 8;
+    sl->timing.rung_ms = rung_ms; sl->timing.direct_ms = direct_ms;
+    sl->timing.marks_kernel_launches = persistent ? 1 : n;
+    sl->timing.kernel_launches = launches;
+    sl->timing.mark_items = total_items;
+    sl->timing.survivors = surv_total;
+    sl->timing.primes = prime_total;
     done = true;
   }
   if (!done) return fail(e, ES_ERR_NOMEM, "survivor list kept overflowing");
   for (size_t i = 0; i < n; ++i) {      // the SUMMARY counters (sieve/rung_scan3.cpp:764-772)
-    const WinCount &c = e->h_cnt[i];
+    const WinCount &c = sl->h_cnt[i];
     es_counters &o = per_window[i];
     o.positions = positions_in(e, w[i].lo, w[i].hi);
     if (e->nf == e->ncov) { o.covered = o.positions - c.surv; o.sieved = 0; }
@@ -1163,8 +1197,6 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_K0T, (size_t)std::max<size_t>(nf, 1) * e->Lpad * sizeof(u16)));
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
-  CU(cudaMalloc(&e->d_ctr, 8 * sizeof(unsigned long long)));
-  CU(cudaMalloc(&e->d_status, sizeof(u32)));
   CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
   CU(cudaMalloc(&d_ress, std::max<size_t>(nf, 1) * sizeof(u64)));
   CU(cudaMalloc(&d_g, std::max<size_t>(nf, 1) * sizeof(u32)));
@@ -1179,12 +1211,12 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMemcpy(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(d_inv, oinv.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
   const u64 total = (u64)L * e->ldk;
-  k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
+  k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
                                                                        e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
   CU(cudaGetLastError());
   if (nf) {
     const u64 tt = (u64)nf * e->Lpad;
-    k_transpose_k0<<<(unsigned)((tt + 255) / 256), 256, 0, e->stream>>>(e->d_K0, L, e->ldk, (u32)nf, e->Lpad, e->d_K0T);
+    k_transpose_k0<<<(unsigned)((tt + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_K0, L, e->ldk, (u32)nf, e->Lpad, e->d_K0T);
     CU(cudaGetLastError());
   }
   // Kill masks for short windows: within each phase (covers, then stage-B' primes), the
@@ -1230,22 +1262,22 @@ static es_status build_tables(es_engine *e) {
     CU(cudaMalloc(&e->d_mdesc, std::max<size_t>(md.size(), 1) * sizeof(MaskDesc)));
     CU(cudaMalloc(&e->d_lfil, std::max<size_t>(lfil.size(), 1) * sizeof(u32)));
     CU(cudaMalloc(&d_fmask, std::max<size_t>(nf, 1) * sizeof(int)));
-    CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), e->stream));
+    CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), e->slots[0].stream));
     if (!md.empty()) CU(cudaMemcpy(e->d_mdesc, md.data(), md.size() * sizeof(MaskDesc), cudaMemcpyHostToDevice));
     if (!lfil.empty()) CU(cudaMemcpy(e->d_lfil, lfil.data(), lfil.size() * sizeof(u32), cudaMemcpyHostToDevice));
     if (nf) CU(cudaMemcpy(d_fmask, fmask.data(), nf * sizeof(int), cudaMemcpyHostToDevice));
     if (nf && !md.empty()) {
       const u64 tt = (u64)L * nf;
-      k_build_masks<<<(unsigned)((tt + 255) / 256), 256, 0, e->stream>>>(e->d_K0, L, e->ldk, (u32)nf, d_fmask,
+      k_build_masks<<<(unsigned)((tt + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_K0, L, e->ldk, (u32)nf, d_fmask,
                                                                          e->d_mdesc, e->Wpad, e->d_mtab);
       CU(cudaGetLastError());
     }
-    CU(cudaStreamSynchronize(e->stream));
+    CU(cudaStreamSynchronize(e->slots[0].stream));
     cudaFree(d_fmask);
     CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc))));
   }
-  CU(cudaStreamSynchronize(e->stream));
+  CU(cudaStreamSynchronize(e->slots[0].stream));
   cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
   // occupancy of the marking kernel, for the persistent grid
   // The attribute is per function and process-wide: set it to the largest size any engine
@@ -1260,6 +1292,77 @@ static es_status build_tables(es_engine *e) {
   return ES_OK;
 }
 
+constexpr size_t SERVE_QUEUE_WINDOWS = 1 << 20;   // windows waiting, across requests
+constexpr size_t SERVE_BATCH_WINDOWS = 8192;      // windows per batch a worker takes
+
+// Device bytes a request's windows need in a slot: descriptors, per-window residues and
+// counters, and the survivor-side buffers sized like run_windows sizes them.
+static u64 request_bytes(const es_engine *e, const es_window *w, size_t n) {
+  u64 pos = 0;
+  for (size_t i = 0; i < n; ++i) pos += positions_in(e, w[i].lo, w[i].hi);
+  const u64 surv = std::min<u64>(std::max<u64>(pos / 64, 1024), 1ull << 26);
+  return n * (sizeof(WinDev) + sizeof(ShortWin) + sizeof(WinCount) + 2ull * e->D) +
+         surv * (sizeof(Surv) + 3 * sizeof(u32) + sizeof(RecDev));
+}
+
+// A serving worker owns slot k: whenever its slot is free it takes every queued request
+// that fits one batch (continuous batching -- requests that arrive while other batches run
+// join the next one), runs the batch on its own stream, and hands each request its windows'
+// counters and records. Workers of different slots run their batches concurrently.
+static void serve_worker(es_engine *e, int k) {
+  cudaSetDevice(e->device);
+  Slot *sl = &e->slots[k];
+  for (;;) {
+    std::vector<Request *> batch;
+    {
+      std::unique_lock<std::mutex> lk(e->qmu);
+      e->qcv.wait(lk, [&] { return e->stopping || !e->queue.empty(); });
+      if (e->stopping && e->queue.empty()) return;
+      size_t nw = 0;
+      while (!e->queue.empty() && (batch.empty() || nw + e->queue.front()->w.size() <= SERVE_BATCH_WINDOWS)) {
+        Request *r = e->queue.front();
+        e->queue.pop_front();
+        nw += r->w.size();
+        e->queued_windows -= r->w.size();
+        batch.push_back(r);
+      }
+    }
+    std::vector<es_window> wins;
+    for (Request *r : batch) wins.insert(wins.end(), r->w.begin(), r->w.end());
+    std::vector<es_counters> cnt(wins.size());
+    es_records recs{nullptr, 0};
+    es_status st = ES_OK;
+    std::string err;
+    if (!wins.empty()) {
+      std::lock_guard<std::mutex> lk(sl->mu);
+      st = run_windows(e, sl, wins.data(), wins.size(), ES_SCHED_PERSISTENT, cnt.data(), &recs);
+      if (st != ES_OK) { std::lock_guard<std::mutex> el(e->err_mu); err = e->last_error; }
+    }
+    // split the batch back into its requests (records are sorted by window)
+    size_t w0 = 0, r0 = 0;
+    for (Request *r : batch) {
+      const size_t n = r->w.size();
+      r->st = st;
+      r->err = err;
+      if (st == ES_OK) {
+        r->cnt.assign(cnt.begin() + w0, cnt.begin() + w0 + n);
+        size_t r1 = r0;
+        while (r1 < recs.n && recs.recs[r1].window < w0 + n) ++r1;
+        r->recs.assign(recs.recs + r0, recs.recs + r1);
+        for (es_record &x : r->recs) x.window -= (uint32_t)w0;
+        r0 = r1;
+      }
+      w0 += n;
+    }
+    free(recs.recs);
+    {
+      std::lock_guard<std::mutex> lk(e->qmu);
+      for (Request *r : batch) { r->done = true; e->mem_in_use -= r->mem; }
+    }
+    e->dcv.notify_all();
+  }
+}
+
 }  // namespace es
 
 using namespace es;
@@ -1267,9 +1370,9 @@ using namespace es;
 namespace es {
 // Probes: copy in, one kernel, copy out. Small and synchronous.
 template <typename Launch>
-static es_status probe(es_engine *e, size_t count, size_t in_bytes, const void *in, size_t out_bytes,
+static es_status probe(es_engine *e, Slot *sl, size_t count, size_t in_bytes, const void *in, size_t out_bytes,
                        std::vector<std::pair<void *, size_t>> outs, Launch launch) {
-  std::lock_guard<std::mutex> lk(e->mu);
+  std::lock_guard<std::mutex> lk(sl->mu);
   cudaSetDevice(e->device);
   void *d_in = nullptr;
   std::vector<void *> d_outs(outs.size(), nullptr);
@@ -1277,16 +1380,16 @@ static es_status probe(es_engine *e, size_t count, size_t in_bytes, const void *
   CU(cudaMalloc(&d_in, std::max<size_t>(in_bytes, 8)));
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMalloc(&d_outs[i], std::max<size_t>(outs[i].second, 8)));
   CU(cudaMemcpy(d_in, in, in_bytes, cudaMemcpyHostToDevice));
-  CU(cudaMemsetAsync(e->d_status, 0, sizeof(u32), e->stream));
-  CU(cudaEventRecord(e->ev[9], e->stream));
+  CU(cudaMemsetAsync(sl->d_status, 0, sizeof(u32), sl->stream));
+  CU(cudaEventRecord(sl->ev[9], sl->stream));
   launch(d_in, d_outs);
   CU(cudaGetLastError());
-  CU(cudaEventRecord(e->ev[10], e->stream));
-  CU(cudaStreamSynchronize(e->stream));
-  e->timing.total_ms = ev_ms(e->ev[9], e->ev[10]);   // the probe kernel alone
+  CU(cudaEventRecord(sl->ev[10], sl->stream));
+  CU(cudaStreamSynchronize(sl->stream));
+  sl->timing.total_ms = ev_ms(sl->ev[9], sl->ev[10]);   // the probe kernel alone
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMemcpy(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost));
   u32 st = 0;
-  CU(cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(&st, sl->d_status, sizeof st, cudaMemcpyDeviceToHost));
   cudaFree(d_in);
   for (void *p : d_outs) cudaFree(p);
   (void)count;
@@ -1389,8 +1492,21 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   }
   if (cudaSetDevice(e->device) != cudaSuccess) { delete e; return ES_ERR_CUDA; }
   cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device);
-  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) { delete e; return ES_ERR_CUDA; }
-  for (auto &ev : e->ev) cudaEventCreate(&ev);
+  for (Slot &sl : e->slots) {
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&sl.d_ctr, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&sl.d_status, sizeof(u32)) != cudaSuccess) {
+      g_open_error = "stream or counter allocation failed";
+      es_close(e);
+      return ES_ERR_CUDA;
+    }
+    for (auto &ev : sl.ev) cudaEventCreate(&ev);
+  }
+  {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    e->mem_budget = cfg->mem_budget ? cfg->mem_budget : fr / 4;   // serving admission budget
+  }
   const es_status s = build_tables(e);
   if (s != ES_OK) {
     g_open_error = e->last_error;
@@ -1403,41 +1519,52 @@ es_status es_open(const es_config *cfg, es_engine **out) {
 
 es_status es_close(es_engine *e) {
   if (!e) return ES_OK;
-  if (e->stream) cudaStreamSynchronize(e->stream);
+  {
+    std::lock_guard<std::mutex> lk(e->qmu);
+    e->stopping = true;
+  }
+  e->qcv.notify_all();
+  for (std::thread &t : e->workers) t.join();
+  for (auto &kv : e->reqs) delete kv.second;
+  cudaSetDevice(e->device);
+  for (Slot &sl : e->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    drop_graph(&sl);
+    cudaFree(sl.d_win); cudaFree(sl.d_cnt); cudaFree(sl.d_shortw); cudaFree(sl.d_Qm);
+    cudaFree(sl.d_surv); cudaFree(sl.d_primes); cudaFree(sl.d_direct); cudaFree(sl.d_recs); cudaFree(sl.d_cand);
+    cudaFree(sl.d_ctr); cudaFree(sl.d_status); cudaFree(sl.d_hdr);
+    cudaFreeHost(sl.h_hdr); cudaFreeHost(sl.h_win); cudaFreeHost(sl.h_short); cudaFreeHost(sl.h_cnt);
+    cudaFreeHost(sl.h_ctr); cudaFreeHost(sl.h_status); cudaFreeHost(sl.h_recs);
+    for (auto &ev : sl.ev) if (ev) cudaEventDestroy(ev);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_Qm); cudaFree(e->d_tde);
-  cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil); cudaFree(e->d_shortw); cudaFree(e->d_win); cudaFree(e->d_cnt);
-  cudaFree(e->d_surv); cudaFree(e->d_primes); cudaFree(e->d_direct); cudaFree(e->d_recs); cudaFree(e->d_cand);
-  cudaFree(e->d_ctr); cudaFree(e->d_status); cudaFree(e->d_hdr);
-  drop_graph(e);
-  cudaFreeHost(e->h_hdr); cudaFreeHost(e->h_win); cudaFreeHost(e->h_short); cudaFreeHost(e->h_cnt);
-  cudaFreeHost(e->h_ctr); cudaFreeHost(e->h_status); cudaFreeHost(e->h_recs);
-  for (auto &ev : e->ev) if (ev) cudaEventDestroy(ev);
-  if (e->stream) cudaStreamDestroy(e->stream);
+  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_tde);
+  cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil);
   delete e;
   return ES_OK;
 }
 
 es_status es_run_window(es_engine *e, uint64_t lo, uint64_t hi, es_counters *out, es_records *recs) {
   if (!e || !out) return ES_ERR_ARG;
-  std::lock_guard<std::mutex> lk(e->mu);
+  std::lock_guard<std::mutex> lk(e->slots[0].mu);
   cudaSetDevice(e->device);
   es_window w{lo, hi};
   memset(out, 0, sizeof *out);
   if (recs) { recs->recs = nullptr; recs->n = 0; }
-  return run_windows(e, &w, 1, ES_SCHED_PERSISTENT, out, recs);
+  return run_windows(e, &e->slots[0], &w, 1, ES_SCHED_PERSISTENT, out, recs);
 }
 
 es_status es_run_batch(es_engine *e, const es_window *w, size_t n, int schedule, es_counters *per_window,
                        es_records *recs) {
   if (!e || (!w && n) || !per_window) return ES_ERR_ARG;
   if (schedule != ES_SCHED_PLAIN && schedule != ES_SCHED_PERSISTENT) return ES_ERR_ARG;
-  std::lock_guard<std::mutex> lk(e->mu);
+  std::lock_guard<std::mutex> lk(e->slots[0].mu);
   cudaSetDevice(e->device);
   memset(per_window, 0, n * sizeof(es_counters));
   if (recs) { recs->recs = nullptr; recs->n = 0; }
   if (n == 0) return ES_OK;
-  return run_windows(e, w, n, schedule, per_window, recs);
+  return run_windows(e, &e->slots[0], w, n, schedule, per_window, recs);
 }
 
 es_status es_free_records(es_records *r) {
@@ -1513,59 +1640,111 @@ es_status es_classes(const es_engine *e, uint64_t *out, size_t cap) {
 
 es_status es_timing(const es_engine *e, es_timing_t *o) {
   if (!e || !o) return ES_ERR_ARG;
-  *o = e->timing;
+  *o = e->slots[0].timing;
   return ES_OK;
 }
 
 es_status es_is_prime_batch(es_engine *e, const uint64_t *n, size_t count, uint8_t *out) {
   if (!e || (!n && count) || (!out && count)) return ES_ERR_ARG;
   if (!count) return ES_OK;
-  return probe(e, count, count * 8, n, count, {{out, count}}, [&](void *in, std::vector<void *> &o) {
-    k_probe_prime<<<e->sm_count * 2, 256, 0, e->stream>>>((const u64 *)in, count, (unsigned char *)o[0]);
+  return probe(e, &e->slots[0], count, count * 8, n, count, {{out, count}}, [&](void *in, std::vector<void *> &o) {
+    k_probe_prime<<<e->sm_count * 2, 256, 0, e->slots[0].stream>>>((const u64 *)in, count, (unsigned char *)o[0]);
   });
 }
 
 es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_record *out, uint8_t *found) {
   if (!e || (!p && count) || (!out && count) || (!found && count)) return ES_ERR_ARG;
   if (!count) return ES_OK;
-  return probe(e, count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
+  return probe(e, &e->slots[0], count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
                [&](void *in, std::vector<void *> &o) {
-                 k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
+                 k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->slots[0].stream>>>((const u64 *)in, count, (RecDev *)o[0],
                                                                      (unsigned char *)o[1], e->d_tdp, e->d_tde,
-                                                                     e->d_status);
+                                                                     e->slots[0].d_status);
                });
 }
 
 es_status es_solve_direct_batch(es_engine *e, const uint64_t *p, size_t count, es_record *out, uint8_t *found) {
   if (!e || (!p && count) || (!out && count) || (!found && count)) return ES_ERR_ARG;
   if (!count) return ES_OK;
-  return probe(e, count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
+  return probe(e, &e->slots[0], count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
                [&](void *in, std::vector<void *> &o) {
-                 k_probe_direct<<<e->sm_count * 4, 32, 0, e->stream>>>((const u64 *)in, count, (RecDev *)o[0],
+                 k_probe_direct<<<e->sm_count * 4, 32, 0, e->slots[0].stream>>>((const u64 *)in, count, (RecDev *)o[0],
                                                                        (unsigned char *)o[1], e->d_tdp, e->d_tde,
-                                                                       e->d_status);
+                                                                       e->slots[0].d_status);
                });
 }
 
 es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_t *pr, uint8_t *ex, uint8_t *k) {
   if (!e || (!n && count) || (!pr && count) || (!ex && count) || (!k && count)) return ES_ERR_ARG;
   if (!count) return ES_OK;
-  return probe(e, count, count * 8, n, 0, {{pr, count * MAXF * 8}, {ex, count * MAXF}, {k, count}},
+  return probe(e, &e->slots[0], count, count * 8, n, 0, {{pr, count * MAXF * 8}, {ex, count * MAXF}, {k, count}},
                [&](void *in, std::vector<void *> &o) {
-                 k_probe_factor<<<e->sm_count * 4, 128, 0, e->stream>>>((const u64 *)in, count, (u64 *)o[0],
+                 k_probe_factor<<<e->sm_count * 4, 128, 0, e->slots[0].stream>>>((const u64 *)in, count, (u64 *)o[0],
                                                                        (unsigned char *)o[1], (unsigned char *)o[2],
-                                                                       e->d_tdp, e->d_tde, e->d_status);
+                                                                       e->d_tdp, e->d_tde, e->slots[0].d_status);
                });
 }
 
 es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket) {
-  (void)w; (void)n; (void)ticket;
-  return e ? fail(e, ES_ERR_ARG, "serving queue not built yet") : ES_ERR_ARG;
+  if (!e || !ticket || (!w && n)) return ES_ERR_ARG;
+  *ticket = 0;
+  const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
+  for (size_t i = 0; i < n; ++i) {                 // refuse what a run would refuse, now
+    if (w[i].hi > DIRECT_PMAX) return fail(e, ES_ERR_RANGE, "HI above the stage-E ceiling");
+    if (w[i].lo <= floor_) return fail(e, ES_ERR_RANGE, "LO at or below the pmin floor");
+  }
+  Request *r = new (std::nothrow) Request();
+  if (!r) return ES_ERR_NOMEM;
+  r->w.assign(w, w + n);
+  r->mem = request_bytes(e, w, n);
+  {
+    std::lock_guard<std::mutex> lk(e->qmu);
+    if (e->stopping) { delete r; return ES_ERR_ARG; }
+    // admission: a bounded queue, and device memory for the request's buffers within the
+    // engine's budget (what is queued or in flight counts against it)
+    if (e->queued_windows + n > SERVE_QUEUE_WINDOWS || e->mem_in_use + r->mem > e->mem_budget) {
+      delete r;
+      return fail(e, ES_ERR_BUSY, "admission refused: queue or device-memory budget full");
+    }
+    if (e->workers.empty())
+      for (int k = 1; k <= SERVE_SLOTS; ++k) e->workers.emplace_back(serve_worker, e, k);
+    r->ticket = e->next_ticket++;
+    e->mem_in_use += r->mem;
+    e->queued_windows += n;
+    e->reqs[r->ticket] = r;
+    e->queue.push_back(r);
+    *ticket = r->ticket;
+  }
+  e->qcv.notify_one();
+  return ES_OK;
 }
 
 es_status es_poll(es_engine *e, uint64_t ticket, es_counters *per_window, es_records *recs, int timeout_ms) {
-  (void)ticket; (void)per_window; (void)recs; (void)timeout_ms;
-  return e ? fail(e, ES_ERR_ARG, "serving queue not built yet") : ES_ERR_ARG;
+  if (!e) return ES_ERR_ARG;
+  if (recs) { recs->recs = nullptr; recs->n = 0; }
+  std::unique_lock<std::mutex> lk(e->qmu);
+  auto it = e->reqs.find(ticket);
+  if (it == e->reqs.end()) return fail(e, ES_ERR_ARG, "unknown ticket");
+  Request *r = it->second;
+  auto ready = [&] { return r->done; };
+  if (timeout_ms < 0) e->dcv.wait(lk, ready);
+  else if (!e->dcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return ES_ERR_TIMEOUT;
+  e->reqs.erase(it);
+  lk.unlock();
+  const es_status st = r->st;
+  if (st == ES_OK) {
+    if (per_window) memcpy(per_window, r->cnt.data(), r->cnt.size() * sizeof(es_counters));
+    if (recs) {
+      recs->n = r->recs.size();
+      recs->recs = (es_record *)malloc(std::max<size_t>(r->recs.size(), 1) * sizeof(es_record));
+      if (!recs->recs) { delete r; return ES_ERR_NOMEM; }
+      memcpy(recs->recs, r->recs.data(), r->recs.size() * sizeof(es_record));
+    }
+  } else {
+    fail(e, st, r->err);
+  }
+  delete r;
+  return st;
 }
 
 }  // extern "C"

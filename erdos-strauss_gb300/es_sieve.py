@@ -146,7 +146,7 @@ def format_record(rec):
 
 
 class Engine:
-    def __init__(self, wheel=2042040, mmax=10000, sieve_p=0, filters=None, device=0, no_rung=False):
+    def __init__(self, wheel=2042040, mmax=10000, sieve_p=0, filters=None, device=0, no_rung=False, mem_budget=0):
         """filters: None (the generated default set), a filter-file path, or (mods, ress)."""
         self.lib = load_library()
         if isinstance(filters, str):
@@ -154,6 +154,7 @@ class Engine:
         cfg = Config()
         cfg.wheel_M, cfg.mmax, cfg.sieve_p, cfg.device = wheel, mmax, sieve_p, device
         cfg.flags = 1 if no_rung else 0
+        cfg.mem_budget = mem_budget
         self._keep = None
         if filters is not None:
             mods = np.ascontiguousarray(filters[0], dtype=np.uint64)
@@ -248,6 +249,22 @@ class Engine:
         nrec = r.n
         self.lib.es_free_records(C.byref(r))
         return nrec
+
+    # ------------------------------------------------------------------ serving
+    def submit(self, windows):
+        """Queue windows; returns a ticket. Raises EsError(ES_ERR_BUSY) when admission is refused."""
+        n = len(windows)
+        w = (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        t = C.c_uint64()
+        self._check(self.lib.es_submit(self.h, w, n, C.byref(t)))
+        return t.value
+
+    def poll(self, ticket, n, timeout_ms=-1):
+        """(per-window counters, records) of a submitted request; EsError(ES_ERR_TIMEOUT) if not done."""
+        c = (Counters * max(n, 1))()
+        r = Records()
+        self._check(self.lib.es_poll(self.h, ticket, c, C.byref(r), timeout_ms))
+        return [c[i].as_dict() for i in range(n)], self._take_records(self.lib, r)
 
     def summary(self, lo, hi, counters):
         c = Counters(*[counters[n] for n in COUNTER_NAMES])

@@ -148,7 +148,15 @@ es_status es_run_batch(es_engine *engine, const es_window *w, size_t n, int sche
                        es_counters *per_window, es_records *recs);
 
 /* Serving: queue windows for verification without waiting; collect them by ticket.
- * Admission is by free slots and device memory (ES_ERR_BUSY when full). No reference
+ * Requests are batched continuously: whenever one of the engine's serving streams frees up,
+ * it takes every queued request that fits its next batch, so requests that arrive while
+ * others run join the next batch and batches on different streams overlap on the device.
+ * Admission: ES_ERR_BUSY when the queue is full or the request's device-memory estimate does
+ * not fit the engine's budget (es_config.mem_budget; 0 = a quarter of the free memory at
+ * es_open); ES_ERR_RANGE at once for a window the run would refuse. es_poll waits up to
+ * timeout_ms (negative: without limit; 0: just checks) and returns ES_ERR_TIMEOUT if the
+ * request is not done; otherwise it fills per_window (one entry per submitted window) and
+ * recs (window indices relative to the request) and forgets the ticket. No reference
  * counterpart. */
 es_status es_submit(es_engine *engine, const es_window *w, size_t n, uint64_t *ticket);
 es_status es_poll(es_engine *engine, uint64_t ticket, es_counters *per_window, es_records *recs,
