@@ -95,49 +95,109 @@ def allsum(ws, v):
 
 
 class Clocks:
-    """nvidia-smi samples every 200 ms during the timed region."""
+    """SM clock and clock-event reasons of the GPU, sampled during the timed region.
+
+    NVML through ctypes every 2 ms (the timed region of a default run is tens of ms), falling
+    back to nvidia-smi every 200 ms. The GPU is found by its PCI bus id, so the sample is of
+    the device the engine runs on whatever CUDA_VISIBLE_DEVICES says. Reads only."""
+    REASONS = ((0x4, "sw_power_cap"), (0x8, "hw_slowdown"), (0x20, "sw_thermal_slowdown"),
+               (0x40, "hw_thermal_slowdown"), (0x80, "hw_power_brake_slowdown"))
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
         self.device = device
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.busid = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(device)
+            self.busid = "%08X:%02X:%02X.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except Exception:
+            pass
+        self.samples, self.max_mhz, self.source = [], None, None
+        self.stop = None
         self.p = None
 
+    def _nvml(self):
+        import ctypes as C
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit")
+        h = C.c_void_p()
+        if self.busid:
+            st = lib.nvmlDeviceGetHandleByPciBusId_v2(self.busid.encode(), C.byref(h))
+        else:
+            st = lib.nvmlDeviceGetHandleByIndex_v2(self.device, C.byref(h))
+        if st != 0:
+            raise OSError("nvml handle")
+        return C, lib, h
+
     def __enter__(self):
+        import threading
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
-                                      stderr=subprocess.DEVNULL)
-        except OSError:
-            self.p = None
+            C, lib, h = self._nvml()
+            mx = C.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.stop = threading.Event()
+
+            def loop():
+                mhz, rs = C.c_uint(), C.c_ulonglong()
+                while not self.stop.is_set():
+                    if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(mhz)) == 0 and reasons_fn(h, C.byref(rs)) == 0:
+                        self.samples.append((float(mhz.value), int(rs.value)))
+                    time.sleep(0.002)
+            self.th = threading.Thread(target=loop, daemon=True)
+            self.th.start()
+            self.source = "nvml 2 ms"
+        except (OSError, AttributeError):
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            try:
+                self.p = subprocess.Popen(["nvidia-smi", "-i", self.busid or str(self.device),
+                                           "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                           "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                self.source = "nvidia-smi 200 ms"
+            except OSError:
+                self.p = None
         return self
 
     def __exit__(self, *a):
+        if self.stop is not None:
+            self.stop.set()
+            self.th.join()
         if self.p:
             self.p.terminate()
             self.p.wait()
 
-    def summary(self):
+    def _smi_rows(self):
         self.f.flush()
         rows = []
         for ln in open(self.f.name):
             t = [x.strip() for x in ln.split(",")]
-            if len(t) >= 9:
-                rows.append(t)
+            if len(t) >= 9 and t[1].replace(".", "").isdigit():
+                bits = 0
+                for (bit, _), val in zip(((0x8, 0), (0x40, 0), (0x20, 0), (0x4, 0)), t[5:9]):
+                    if val.lower().startswith("active"):
+                        bits |= bit
+                rows.append((float(t[1]), bits))
+                if t[2].replace(".", "").isdigit():
+                    self.max_mhz = max(self.max_mhz or 0.0, float(t[2]))
         os.unlink(self.f.name)
+        return rows
+
+    def summary(self):
+        rows = self.samples if self.stop is not None else (self._smi_rows() if self.p else [])
         if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
-        for r in rows:
-            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[5:9]):
-                if val.lower().startswith("active"):
-                    reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0}
+        seen = 0
+        for _, bits in rows:
+            seen |= bits
+        return {"sm_mhz": statistics.median(m for m, _ in rows), "sm_max_mhz": self.max_mhz,
+                "reasons": [name for bit, name in self.REASONS if seen & bit], "samples": len(rows),
+                "source": self.source}
 
 
 def peaks():

@@ -39,6 +39,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace es {
@@ -316,40 +317,91 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 constexpr int SHORT_LANES = 2;
 constexpr u32 SMD_MAX = 512;       // stride descriptors staged in shared memory
 
-// kill[q][c] gets bit j set when position 32c + j of lane q's segment is killed by a mask
-// stride in [m0, m1) or by a filter of lfil[l0, l1). A segment starts at K == Qrow[d] + b[q]
-// (mod s_d) and has n[q] positions (0: lane inactive). Mask bits come out 32 at a time: word
-// r/32 and the next, funnel-shifted right by r mod 32. Lanes of the warp split the strides;
-// the caller reduces.
+__device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFFFFFFu, v); }
+
+// Mask strides [m0, m1) over the segments of SHORT_LANES lanes, in rounds of 32 strides (one
+// per lane of the warp). alive[q][c] holds the positions 32c + j of lane q's segment not yet
+// killed; it is the same in every lane of the warp. A segment starts at K == Qrow[d] + b[q]
+// (mod s_d); mask bits come out 32 at a time: word r/32 + c and the next, funnel-shifted right
+// by r mod 32. After each round the warp ORs its kill words into alive, and it stops as soon
+// as nothing is left alive: the strides come densest first, so most segments are dead after
+// one or two rounds. Returns nonzero if a position is still alive.
+__device__ __forceinline__ MaskDesc mask_desc(const MaskDesc *smd, const MaskDesc *__restrict__ mdesc, u32 k) {
+  if (smd) return smd[k];
+  const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k);
+  return MaskDesc{mv.x, mv.y, mv.z, mv.w};
+}
+
 template <int NC>
-__device__ __forceinline__ void short_kill(u32 (&kill)[SHORT_LANES][NC], const u32 (&n)[SHORT_LANES],
-                                           const u32 (&b)[SHORT_LANES], const u32 *tab, u32 tab_words,
-                                           const MaskDesc *smd, const MaskDesc *__restrict__ mdesc, u32 m0,
-                                           u32 m1, const u32 *__restrict__ lfil, u32 l0, u32 l1,
-                                           const u16 *const (&K0row)[SHORT_LANES], const u32 *__restrict__ fdesc,
-                                           const u16 *__restrict__ Qrow, u32 lane) {
-  for (u32 k = m0 + lane; k < m1; k += 32) {
-    MaskDesc md;
-    if (smd) md = smd[k];
-    else { const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k); md = MaskDesc{mv.x, mv.y, mv.z, mv.w}; }
-    const u32 s = md.s;
-    const u32 q0 = (u32)__ldg(Qrow + md.d);
+__device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], const u32 (&b)[SHORT_LANES],
+                                                 const u32 *tab, u32 tab_words, const MaskDesc *smd,
+                                                 const MaskDesc *__restrict__ mdesc, u32 m0, u32 m1,
+                                                 const u16 *__restrict__ Qrow, u32 q0_first, u32 lane) {
+  u32 any = 0;
+  #pragma unroll
+  for (int q = 0; q < SHORT_LANES; ++q)
     #pragma unroll
-    for (int q = 0; q < SHORT_LANES; ++q) {
-      u32 r = q0 + b[q];
-      r = r >= s ? r - s : r;
-      // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
-      const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
-      const u32 sh = r & 31;
-      u32 w0 = wp[0];
+    for (int c = 0; c < NC; ++c) any |= alive[q][c];
+  // q0_first: this lane's segment-start residue for stride m0 + lane, loaded by the caller
+  // ahead of time; each round loads the next round's while it works
+  u32 q0 = q0_first;
+  for (u32 kb = m0; kb < m1 && any; kb += 32) {
+    u32 kill[SHORT_LANES][NC];
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
       #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const u32 w1 = wp[c + 1];
-        kill[q][c] |= __funnelshift_r(w0, w1, sh);
-        w0 = w1;
+      for (int c = 0; c < NC; ++c) kill[q][c] = 0;
+    const u32 k = kb + lane;
+    u32 q0_next = 0;
+    if (k + 32 < m1) q0_next = (u32)__ldg(Qrow + mask_desc(smd, mdesc, k + 32).d);
+    if (k < m1) {
+      const MaskDesc md = mask_desc(smd, mdesc, k);
+      const u32 s = md.s;
+      #pragma unroll
+      for (int q = 0; q < SHORT_LANES; ++q) {
+        u32 r = q0 + b[q];
+        r = r >= s ? r - s : r;
+        // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
+        const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+        const u32 sh = r & 31;
+        if (kb == m0) {                       // first round: every chunk, one load each
+          u32 w0 = wp[0];
+          #pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            const u32 w1 = wp[c + 1];
+            kill[q][c] = __funnelshift_r(w0, w1, sh);
+            w0 = w1;
+          }
+        } else {                              // later rounds: only the chunks still alive
+          #pragma unroll
+          for (int c = 0; c < NC; ++c)
+            if (alive[q][c]) kill[q][c] = __funnelshift_r(wp[c], wp[c + 1], sh);
+        }
       }
     }
+    q0 = q0_next;
+    any = 0;
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (alive[q][c]) {
+          alive[q][c] &= ~warp_or32(kill[q][c]);
+          any |= alive[q][c];
+        }
   }
+  return any;
+}
+
+// kill[q][c] gets bit j set when position 32c + j of lane q's segment is hit by one of the
+// filters lfil[l0, l1) (the strides without a mask), checked one by one from the first-hit
+// table. Lanes of the warp split the filters; the caller reduces.
+template <int NC>
+__device__ __forceinline__ void short_list_kill(u32 (&kill)[SHORT_LANES][NC], const u32 (&n)[SHORT_LANES],
+                                                const u32 (&b)[SHORT_LANES], const u32 *__restrict__ lfil, u32 l0,
+                                                u32 l1, const u16 *const (&K0row)[SHORT_LANES],
+                                                const u32 *__restrict__ fdesc, const u16 *__restrict__ Qrow,
+                                                u32 lane) {
   for (u32 k = l0 + lane; k < l1; k += 32) {
     const u32 f = lfil[k];
     const u32 fd = __ldg(fdesc + f);
@@ -372,7 +424,35 @@ __device__ __forceinline__ void short_kill(u32 (&kill)[SHORT_LANES][NC], const u
   }
 }
 
-__device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFFFFFFu, v); }
+// One phase (covers, or the stage-B' primes) over alive: the mask strides [m0, m1), then, if
+// anything survived them, the unmasked filters lfil[l0, l1). Returns the positions alive.
+template <int NC>
+__device__ __forceinline__ u32 short_phase(u32 (&alive)[SHORT_LANES][NC], const ShortParams &P, const u32 *tab,
+                                           u32 tab_words, const MaskDesc *smd, u32 m0, u32 m1, u32 l0, u32 l1,
+                                           const u32 (&n)[SHORT_LANES], const u32 (&b)[SHORT_LANES],
+                                           const u16 *const (&K0row)[SHORT_LANES], const u16 *Qrow, u32 q0_first,
+                                           u32 lane) {
+  const u32 any = short_mask_rounds<NC>(alive, b, tab, tab_words, smd, P.mdesc, m0, m1, Qrow, q0_first, lane);
+  if (any && l1 > l0) {
+    u32 kill[SHORT_LANES][NC];
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) kill[q][c] = 0;
+    short_list_kill<NC>(kill, n, b, P.lfil, l0, l1, K0row, P.fdesc, Qrow, lane);
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) alive[q][c] &= ~warp_or32(kill[q][c]);
+  }
+  u32 cnt = 0;
+  #pragma unroll
+  for (int q = 0; q < SHORT_LANES; ++q)
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) cnt += __popc(alive[q][c]);
+  return cnt;
+}
+
 
 // The segments of SHORT_LANES lanes in one short window, NC 32-position chunks each.
 template <int NC>
@@ -380,42 +460,24 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
                                                const MaskDesc *smd, u32 l_first, u32 wi,
                                                const u64 (&first)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
                                                const u32 (&b)[SHORT_LANES], const u16 *const (&K0row)[SHORT_LANES],
-                                               u32 lane) {
+                                               u32 q0_first, u32 lane) {
   const u16 *Qrow = P.Qm + (size_t)wi * P.D;
-  u32 kill[SHORT_LANES][NC];
-  #pragma unroll
-  for (int q = 0; q < SHORT_LANES; ++q)
-    #pragma unroll
-    for (int c = 0; c < NC; ++c) kill[q][c] = 0;
-  short_kill<NC>(kill, n, b, tab, tab_words, smd, P.mdesc, 0, P.nm_cov, P.lfil, 0, P.nl_cov, K0row, P.fdesc, Qrow,
-                 lane);
   u32 alive[SHORT_LANES][NC];
-  u32 cnt = 0;
   #pragma unroll
   for (int q = 0; q < SHORT_LANES; ++q)
     #pragma unroll
     for (int c = 0; c < NC; ++c) {
       const u32 lo = 32 * c;
-      const u32 valid = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
-      alive[q][c] = valid & ~warp_or32(kill[q][c]);
-      cnt += __popc(alive[q][c]);
+      alive[q][c] = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
     }
-  if (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov) {                  // stage B'
-    if (lane == 0 && cnt) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
-    #pragma unroll
-    for (int q = 0; q < SHORT_LANES; ++q)
-      #pragma unroll
-      for (int c = 0; c < NC; ++c) kill[q][c] = 0;
-    short_kill<NC>(kill, n, b, tab, tab_words, smd, P.mdesc, P.nm_cov, P.nm_all, P.lfil, P.nl_cov, P.nl_all,
-                   K0row, P.fdesc, Qrow, lane);
-    cnt = 0;
-    #pragma unroll
-    for (int q = 0; q < SHORT_LANES; ++q)
-      #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        alive[q][c] &= ~warp_or32(kill[q][c]);
-        cnt += __popc(alive[q][c]);
-      }
+  u32 cnt = short_phase<NC>(alive, P, tab, tab_words, smd, 0, P.nm_cov, 0, P.nl_cov, n, b, K0row, Qrow, q0_first,
+                            lane);
+  if (cnt && (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov)) {          // stage B'
+    if (lane == 0) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
+    const u32 k = P.nm_cov + lane;
+    const u32 q0b = k < P.nm_all ? (u32)__ldg(Qrow + mask_desc(smd, P.mdesc, k).d) : 0u;
+    cnt = short_phase<NC>(alive, P, tab, tab_words, smd, P.nm_cov, P.nm_all, P.nl_cov, P.nl_all, n, b, K0row, Qrow,
+                          q0b, lane);
   }
   if (cnt && lane == 0) {              // survivors are rare: lane 0 writes them in order
     u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
@@ -471,8 +533,31 @@ __global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
       rho[q] = P.rho[l];
       K0row[q] = P.K0 + (size_t)l * P.ldk;
     }
-    for (u32 i = warp; i < nshort; i += BLOCK / 32) {
-      const ShortWin W = P.shortw[i];
+    // Software pipeline over this warp's windows: the descriptor two windows ahead and the
+    // first round's stride residue one window ahead are in flight while a window is marked.
+    constexpr u32 WS = BLOCK / 32;
+    const uint4 *sw4 = reinterpret_cast<const uint4 *>(P.shortw);
+    auto load_win = [&](u32 i) {
+      ShortWin W{};
+      if (i < nshort) {
+        const uint4 x = __ldg(sw4 + 2 * (size_t)i), y = __ldg(sw4 + 2 * (size_t)i + 1);
+        W.Q = (u64)x.x | ((u64)x.y << 32);
+        W.lomod = x.z; W.wi = x.w; W.la = y.x; W.lb = y.y; W.lq = y.z; W.lr = y.w;
+      }
+      return W;
+    };
+    const u32 d_first = lane < P.nm_cov ? mask_desc(smd, P.mdesc, lane).d : 0u;
+    auto load_q0 = [&](u32 i, const ShortWin &W) {
+      return (i < nshort && lane < P.nm_cov) ? (u32)__ldg(P.Qm + (size_t)W.wi * P.D + d_first) : 0u;
+    };
+    ShortWin Wn = load_win(warp), Wnn = load_win(warp + WS);
+    u32 q0n = load_q0(warp, Wn);
+    for (u32 i = warp; i < nshort; i += WS) {
+      const ShortWin W = Wn;
+      const u32 q0_first = q0n;
+      Wn = Wnn;
+      Wnn = load_win(i + 2 * WS);
+      q0n = load_q0(i + WS, Wn);
       u64 first[SHORT_LANES];
       u32 n[SHORT_LANES], b[SHORT_LANES];
       u32 nmax = 0;
@@ -489,14 +574,14 @@ __global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
       #pragma unroll
       for (int q = 0; q < SHORT_LANES; ++q) first[q] = rho[q] + P.M * (W.Q + b[q]);
       switch ((nmax + 31) >> 5) {
-        case 1: short_segments<1>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 2: short_segments<2>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 3: short_segments<3>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 4: short_segments<4>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 5: short_segments<5>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 6: short_segments<6>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        case 7: short_segments<7>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
-        default: short_segments<8>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, lane); break;
+        case 1: short_segments<1>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 2: short_segments<2>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 3: short_segments<3>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 4: short_segments<4>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 5: short_segments<5>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 6: short_segments<6>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        case 7: short_segments<7>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+        default: short_segments<8>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
       }
     }
     __syncthreads();
@@ -563,7 +648,10 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
 
 constexpr int RUNG_WARPS = 4;
 
-// Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung).
+// Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung). Blocks take primes
+// from a queue; a block that finds it empty turns its warps into helpers on the hard board
+// (warp_help) until every prime of the run is finished, so that the last, hardest
+// factorizations of a run get the walks of every idle warp instead of one warp's.
 __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T, int no_rung) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
@@ -571,12 +659,19 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
   __shared__ int best_k;
   __shared__ RungResult slot[RUNG_WARPS];
   __shared__ RungResult res;
+  __shared__ unsigned long long next;
   const u64 n = min((u64)*T.prime_count, T.cap);
-  for (u64 i = blockIdx.x; i < n; i += gridDim.x) {
+  HardBoard B;
+  B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
+  for (;;) {
+    if (threadIdx.x == 0) next = atomicAdd(T.rung_next, 1ull);
+    __syncthreads();
+    const u64 i = next;
+    if (i >= n) break;
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
     const bool ok = !no_rung &&
-                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res);
+                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B);
     if (threadIdx.x == 0) {
       if (ok) {
         RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, res.A, res.r, res.u.lo, res.u.hi};
@@ -586,9 +681,12 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
         const unsigned long long k = atomicAdd(T.direct_count, 1ull);
         if (k < T.cap) T.direct[k] = si;
       }
+      __threadfence();
+      atomicAdd(T.rung_done, 1ull);
     }
     __syncthreads();
   }
+  if (!no_rung) warp_help(B, threadIdx.x & 31);
 }
 
 __global__ void k_direct(const TailParams T) {
@@ -705,12 +803,15 @@ struct Slot {
   RecDev *d_recs = nullptr;
   size_t cap = 0;
   unsigned long long *d_ctr = nullptr;  // [0] queue [1] surv [2] prime [3] direct [4] rec [5] cand
+                                      // [6] rung queue [7] rungs done [8] help sessions, board at [16]
   u32 *d_status = nullptr;
   es_timing_t timing{};
   std::mutex mu;                        // one run at a time per slot
 };
 
 constexpr int SERVE_SLOTS = 2;
+// run counters (16 words) followed by the hard board, cleared together before every run
+constexpr size_t CTR_BYTES = 16 * sizeof(unsigned long long) + HARD_SLOTS * sizeof(HardSlot);
 
 // A serving request: windows in, counters and records out.
 struct Request {
@@ -848,6 +949,8 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.primes = sl->d_primes; T.prime_count = sl->d_ctr + 2;
   T.direct = sl->d_direct; T.direct_count = sl->d_ctr + 3;
   T.recs = sl->d_recs; T.rec_count = sl->d_ctr + 4;
+  T.rung_next = sl->d_ctr + 6; T.rung_done = sl->d_ctr + 7; T.help_sessions = sl->d_ctr + 8;
+  T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
   T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;
   T.cap = sl->cap;
   return T;
@@ -925,7 +1028,7 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
   auto rec = [&](int k) {
     return capture ? cudaEventRecordWithFlags(sl->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(sl->ev[k], st);
   };
-  CU(cudaMemsetAsync(sl->d_ctr, 0, 8 * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(sl->d_ctr, 0, CTR_BYTES, st));
   CU(cudaMemsetAsync(sl->d_status, 0, sizeof(u32), st));
   CU(cudaMemcpyAsync(sl->d_hdr, sl->h_hdr, sizeof(BatchHdr), cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(sl->d_win, sl->h_win, ncopy * sizeof(WinDev), cudaMemcpyHostToDevice, st));
@@ -1221,11 +1324,27 @@ static es_status build_tables(es_engine *e) {
   }
   // Kill masks for short windows: within each phase (covers, then stage-B' primes), the
   // smallest strides get a mask while the per-lane table fits MASK_BYTES_MAX; the filters of
-  // the remaining strides are checked one by one from the first-hit table.
+  // the remaining strides are checked one by one from the first-hit table. The masked strides
+  // are then ordered by how many positions they kill -- the sum over lanes and filters of
+  // 1/s where the filter hits the lane (rho == res mod g) -- so that k_mark_short, which stops
+  // once a segment is dead, meets the densest strides first. Kills are ORed, so the order
+  // cannot change a result.
   {
     std::vector<MaskDesc> md;
     std::vector<int> fmask(nf, -1);
     std::vector<u32> lfil_cov, lfil_siv;
+    std::map<u32, std::unordered_map<u32, u32>> lanes_mod;     // g -> (rho mod g -> lanes)
+    for (size_t k = 0; k < nf; ++k) {
+      auto &h = lanes_mod[og[k]];
+      if (h.empty())
+        for (u32 l = 0; l < L; ++l) ++h[rho[l] % og[k]];
+    }
+    std::vector<double> kills(65536, 0.0);
+    for (size_t k = 0; k < nf; ++k) {
+      const auto &h = lanes_mod[og[k]];
+      const auto it = h.find((u32)(orr[k] % og[k]));
+      if (it != h.end()) kills[fdesc[k] & 0xFFFFu] += (double)it->second / (double)(fdesc[k] & 0xFFFFu);
+    }
     u32 words = 0;
     for (int phase = 0; phase < 2; ++phase) {
       const size_t f0 = phase ? e->ncov : 0, f1 = phase ? nf : e->ncov;
@@ -1234,16 +1353,19 @@ static es_status build_tables(es_engine *e) {
       std::sort(strides.begin(), strides.end());
       strides.erase(std::unique(strides.begin(), strides.end()), strides.end());
       std::vector<int> slot_of(65536, -1);
+      const size_t m_first = md.size();
       for (u32 st : strides) {
         // bits [0, s + SEG_SMALL) plus one spare word: a segment of up to SEG_SMALL positions
         // starting at any residue below s reads words r/32 .. r/32 + SEG_SMALL/32 of the slice
         const u32 wd = (st + SEG_SMALL + 31) / 32 + 1;
         if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX) break;
         const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
-        slot_of[st] = (int)md.size();
         md.push_back(MaskDesc{st, di, words, 32 % st});
         words += wd;
       }
+      std::stable_sort(md.begin() + m_first, md.end(),
+                       [&](const MaskDesc &x, const MaskDesc &y) { return kills[x.s] > kills[y.s]; });
+      for (size_t m = m_first; m < md.size(); ++m) slot_of[md[m].s] = (int)m;
       for (size_t k = f0; k < f1; ++k) {
         const int m = slot_of[fdesc[k] & 0xFFFFu];
         fmask[k] = m;
@@ -1494,7 +1616,7 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device);
   for (Slot &sl : e->slots) {
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&sl.d_ctr, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&sl.d_ctr, CTR_BYTES) != cudaSuccess ||
         cudaMalloc(&sl.d_status, sizeof(u32)) != cudaSuccess) {
       g_open_error = "stream or counter allocation failed";
       es_close(e);

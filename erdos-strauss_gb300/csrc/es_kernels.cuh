@@ -111,6 +111,8 @@ struct ShortParams {
   u32 L, ldk, D, Wpad, nm_cov, nm_all, nl_cov, nl_all;
 };
 
+struct HardSlot;
+
 struct TailParams {
   Surv *surv;
   unsigned long long *surv_count;
@@ -127,6 +129,10 @@ struct TailParams {
   const TdEntry *tde;
   u32 *status;
   u64 cap;                 // capacity of surv/primes/direct/recs
+  unsigned long long *rung_next;      // k_rung's prime queue head
+  unsigned long long *rung_done;      // primes k_rung has finished
+  unsigned long long *help_sessions;  // helping sessions started on the hard board
+  struct HardSlot *board;             // [HARD_SLOTS] cofactors whose rho takes long
 };
 
 }  // namespace es

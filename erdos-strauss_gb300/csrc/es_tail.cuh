@@ -88,11 +88,13 @@ __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const
 // much as twenty steps here). A 64-bit Montgomery multiply is issue-bound on this GPU (the
 // wide integer multiplies issue at a quarter of the low-half rate), so more walks per lane
 // would only add work: the latency-optimal split is one walk per lane.
-// A walk whose batch product shares all of n backtracks one step at a time from the batch
-// start. Returns a nontrivial factor of the odd composite n (the same value in every lane),
-// or 0 when every lane exhausted its budget. The factorization is unique, so which walk wins
-// cannot change any result.
-constexpr int RHO_WALKS = 1;
+// The lanes run in lockstep (one window schedule for the warp), so that the warp can stop as
+// soon as any lane has a divisor, poll the hard board between batches and be cancelled
+// there. A lane whose batch product shares all of n backtracks one step at a time from the
+// batch start; if that closes without a divisor its walk restarts with its next constant.
+// Returns a nontrivial factor of the odd composite n (the same value in every lane), or 0
+// when the budget ran out or the warp was cancelled. The factorization is unique, so which
+// walk wins cannot change any result.
 constexpr u64 RHO_R0 = 16;      // first comparison window
 constexpr u64 RHO_BATCH = 256;  // steps between gcds
 
@@ -103,87 +105,166 @@ __device__ __forceinline__ bool cancelled(const volatile int *cancel, int my_k) 
   return cancel && *cancel < my_k;
 }
 
-__device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
-                               int my_k = 0) {
-  if (lane == 0) *found = 0;
-  __syncwarp();
-  const Mont M = mont_init(n);
-  u64 result = 0;
-  u64 budget = WARP_RHO_STEPS;
+// The hard board: a cofactor whose rho is still running after RHO_POST_STEPS steps is posted
+// here, and warps with nothing left to do (k_rung blocks that found the prime queue empty) run
+// more walks on it with constants of their own. Any nontrivial divisor ends the search; by the
+// birthday bound the wait for the first collision among W walks shrinks like 1/sqrt(W). The
+// board only speeds things up: the owner checks every divisor it is handed (1 < d < n,
+// n mod d == 0) and its own walks still finish the job alone. No warp ever waits for another.
+constexpr u32 HARD_SLOTS = 32;                 // one per lane of a scanning warp
+constexpr u64 RHO_POST_STEPS = 1024;           // steps per lane before a cofactor is posted
+constexpr u64 HELP_STEPS = 1ull << 16;         // steps per lane of one helping session
+constexpr u32 HELP_IDLE_POLLS = 4096;          // empty-board polls (2 us apart) before a helper leaves
+constexpr u32 HELP_MAX_ROUNDS = 1024;          // board scans (sessions or polls) per helper, at most
+struct HardSlot {
+  unsigned long long n, found;
+  unsigned int state, pad;                     // 0 free, 1 being written, 2 posted
+  unsigned long long pad2;
+};
+struct HardBoard {
+  HardSlot *slot;                              // [HARD_SLOTS], all free between runs
+  unsigned long long *sessions;                // helping sessions started (distinct constants)
+  unsigned long long *done;                    // primes finished by k_rung
+  unsigned long long total;                    // primes k_rung has to finish
+};
+
+__device__ __forceinline__ u64 ld_volatile(const unsigned long long *p) { return *(const volatile unsigned long long *)p; }
+__device__ __forceinline__ u32 ld_volatile(const unsigned int *p) { return *(const volatile unsigned int *)p; }
+
+// The lockstep walk shared by the owner and its helpers. c0: this lane's first constant,
+// cstep: the distance to its next one. poll() is called by every lane between batches (warp-
+// uniform) and returns a divisor handed in from outside, ~0 to stop, or 0 to go on.
+template <class Poll>
+__device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep, u64 budget, u32 lane, Poll poll) {
   const u64 y0 = to_mont(2, M);
-  for (u64 cbase = 1 + lane; cbase < 4096 && result == 0 && *found == 0 && budget && !cancelled(cancel, my_k);
-       cbase += 32 * RHO_WALKS) {
-    u64 cm[RHO_WALKS], y[RHO_WALKS], q[RHO_WALKS], x[RHO_WALKS], ys[RHO_WALKS], g[RHO_WALKS];
-    #pragma unroll
-    for (int w = 0; w < RHO_WALKS; ++w) {
-      cm[w] = to_mont(cbase + 32 * w, M);
-      y[w] = y0; q[w] = M.one; x[w] = 0; ys[w] = 0; g[w] = 1;
-    }
-    bool hit = false;
-    u64 r = RHO_R0;
-    while (!hit && *found == 0 && !cancelled(cancel, my_k)) {
-      #pragma unroll
-      for (int w = 0; w < RHO_WALKS; ++w) x[w] = y[w];
-      if (budget < r) { budget = 0; break; }
-      budget -= r;
-      for (u64 i = 0; i < r; ++i) {
-        #pragma unroll
-        for (int w = 0; w < RHO_WALKS; ++w) y[w] = addmod(mmul(y[w], y[w], M), cm[w], n);
+  u64 c = c0;
+  u64 cm = to_mont(c, M);
+  u64 y = y0, x = y0, ys = y0, q = M.one;
+  u64 steps = 0;
+  for (u64 r = RHO_R0;; r <<= 1) {
+    x = y;
+    if (steps + 2 * r > budget) return 0;
+    for (u64 i = 0; i < r; ++i) y = addmod(mmul(y, y, M), cm, n);
+    steps += r;
+    for (u64 k = 0; k < r; k += RHO_BATCH) {
+      ys = y;
+      const u64 lim = RHO_BATCH < r - k ? RHO_BATCH : r - k;
+      for (u64 i = 0; i < lim; ++i) {
+        y = addmod(mmul(y, y, M), cm, n);
+        q = mmul(q, x > y ? x - y : y - x, M);        // a closed cycle makes q 0
       }
-      for (u64 k = 0; k < r && !hit; k += RHO_BATCH) {
-        #pragma unroll
-        for (int w = 0; w < RHO_WALKS; ++w) ys[w] = y[w];
-        const u64 lim = RHO_BATCH < r - k ? RHO_BATCH : r - k;
-        if (budget < lim) { budget = 0; break; }
-        budget -= lim;
-        for (u64 i = 0; i < lim; ++i) {
-          #pragma unroll
-          for (int w = 0; w < RHO_WALKS; ++w) {
-            y[w] = addmod(mmul(y[w], y[w], M), cm[w], n);
-            q[w] = mmul(q[w], x[w] > y[w] ? x[w] - y[w] : y[w] - x[w], M);   // a closed cycle makes q 0
+      steps += lim;
+      u64 mine = 0;
+      const u64 g = gcd64(q, n);
+      if (g != 1) {
+        if (g != n) mine = g;
+        else {
+          const u64 gb = rho_backtrack(x, ys, cm, n, M);
+          if (gb != 1 && gb != n) mine = gb;
+          else {                                        // this walk is spent: next constant
+            c += cstep;
+            cm = to_mont(c, M);
+            y = y0; x = y0; q = M.one;
           }
         }
-        u64 all = q[0];
-        #pragma unroll
-        for (int w = 1; w < RHO_WALKS; ++w) all = mmul(all, q[w], M);
-        const u64 ga = gcd64(all, n);
-        if (ga != 1) {
-          hit = true;
-          if (RHO_WALKS == 1) g[0] = ga;
-          else {
-            #pragma unroll
-            for (int w = 0; w < RHO_WALKS; ++w) g[w] = gcd64(q[w], n);
-          }
-        }
-        if (*found || cancelled(cancel, my_k)) break;
       }
-      r <<= 1;
-      if (r > (1ull << 26) || budget == 0) break;
+      const unsigned has = __ballot_sync(FULL, mine != 0);
+      if (has) return __shfl_sync(FULL, mine, __ffs(has) - 1);
+      const u64 ext = poll(steps);
+      if (ext) return ext == ~0ull ? 0 : ext;
     }
-    #pragma unroll
-    for (int w = 0; w < RHO_WALKS; ++w)
-      if (!result && g[w] != 1 && g[w] != n) result = g[w];
-    #pragma unroll
-    for (int w = 0; w < RHO_WALKS; ++w)
-      if (!result && g[w] == n) {
-        const u64 gb = rho_backtrack(x[w], ys[w], cm[w], n, M);
-        if (gb != 1 && gb != n) result = gb;
-      }
-    if (result) *found = result;
   }
+}
+
+__device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
+                               int my_k = 0, const HardBoard *board = nullptr) {
+  const Mont M = mont_init(n);
+  int slot = -1;                                   // the board slot this warp posted n in
+  auto poll = [&](u64 steps) -> u64 {
+    u64 ext = 0;
+    if (lane == 0) {
+      if (cancelled(cancel, my_k)) ext = ~0ull;
+      else if (board && slot < 0 && steps >= RHO_POST_STEPS) {
+        for (u32 j = 0; j < HARD_SLOTS; ++j)
+          if (atomicCAS(&board->slot[j].state, 0u, 1u) == 0u) {
+            board->slot[j].n = n;
+            board->slot[j].found = 0;
+            __threadfence();
+            atomicExch(&board->slot[j].state, 2u);
+            slot = (int)j;
+            break;
+          }
+        if (slot < 0) slot = (int)HARD_SLOTS;      // board full: do not try again
+      } else if (board && slot >= 0 && slot < (int)HARD_SLOTS) {
+        const u64 d = ld_volatile(&board->slot[slot].found);
+        if (d > 1 && d < n && n % d == 0) ext = d;
+      }
+    }
+    return __shfl_sync(FULL, ext, 0);
+  };
+  const u64 f = rho_walk(n, M, 1 + lane, 32, WARP_RHO_STEPS, lane, poll);
+  if (lane == 0 && slot >= 0 && slot < (int)HARD_SLOTS) {  // take n off the board
+    atomicExch(&board->slot[slot].state, 1u);
+    board->slot[slot].n = 0;
+    board->slot[slot].found = 0;
+    __threadfence();
+    atomicExch(&board->slot[slot].state, 0u);
+  }
+  if (lane == 0) *found = f;
   __syncwarp();
-  const unsigned has = __ballot_sync(FULL, result != 0);
-  if (has) return __shfl_sync(FULL, result, __ffs(has) - 1);
-  const u64 f = *found;
   if (!f && lane == 0 && !cancelled(cancel, my_k)) atomicOr(status, ST_RHO_BUDGET);
   return f;
+}
+
+// A warp with nothing left to do helps the posted cofactors until every prime of the run is
+// finished (or the board stays empty for HELP_IDLE_POLLS polls, or after HELP_MAX_ROUNDS
+// sessions): each session picks a posted
+// slot, walks HELP_STEPS steps per lane with constants no other walk uses, and posts the
+// first divisor it finds. All lanes call.
+__device__ inline void warp_help(const HardBoard &B, u32 lane) {
+  for (u32 idle = 0, round = 0; idle < HELP_IDLE_POLLS && round < HELP_MAX_ROUNDS + HELP_IDLE_POLLS; ++round) {
+    if (ld_volatile(B.done) >= B.total) return;
+    const u32 st = lane < HARD_SLOTS ? ld_volatile(&B.slot[lane].state) : 0u;
+    const unsigned posted = __ballot_sync(FULL, st == 2u);
+    if (!posted) {
+      ++idle;
+      __nanosleep(2000);
+      continue;
+    }
+    u64 ses = 0;
+    if (lane == 0) ses = atomicAdd(B.sessions, 1ull);
+    ses = __shfl_sync(FULL, ses, 0);
+    u32 pick = (u32)(ses % (u64)__popc(posted)), j = 0;
+    for (unsigned m = posted;; m &= m - 1) {
+      if (pick-- == 0) { j = (u32)(__ffs(m) - 1); break; }
+    }
+    HardSlot *hs = &B.slot[j];
+    const u64 n = ld_volatile(&hs->n);
+    __threadfence();
+    if (ld_volatile(&hs->state) != 2u || n <= 0xFFFFFFFFull || !(n & 1)) continue;
+    const Mont M = mont_init(n);
+    // constants above every owner's (an owner walks c = 1 + lane + 32 j with j far below 2^19),
+    // distinct per session (2^20 sessions apart before a restart adds 2^25)
+    const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
+    auto poll = [&](u64) -> u64 {
+      u64 ext = 0;
+      if (lane == 0)
+        ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
+      return __shfl_sync(FULL, ext, 0);
+    };
+    const u64 d = rho_walk(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll);
+    if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
+      atomicCAS(&hs->found, 0ull, (unsigned long long)d);
+    __syncwarp();
+  }
 }
 
 // Complete factorization of n >= 1 into F (prime order as found). All lanes call.
 // Returns false when a bound was hit (status says which).
 __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
                                    u32 *status, u32 lane, volatile u64 *rho_slot,
-                                   const volatile int *cancel = nullptr, int my_k = 0) {
+                                   const volatile int *cancel = nullptr, int my_k = 0,
+                                   const HardBoard *board = nullptr) {
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
   if (n <= 1) return true;
@@ -262,7 +343,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
         const u64 s = isqrt64(v);
         if (s * s == v) { wf_add(F, s, 2, lane); continue; }
-        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k);
+        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board);
         if (d == 0) return false;                  // budget (status set) or cancelled
         if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
         stack[sp++] = d;
@@ -341,7 +422,8 @@ struct RungResult { u64 A; u32 r, k; U128 u; };
 // thread when some rung certifies p; the block's result is then in *out.
 template <int W>
 __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
-                                 volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out) {
+                                 volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out,
+                                 const HardBoard *board = nullptr) {
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) *best_k = 0x7FFFFFFF;
   if (lane == 0) slot[w].k = 0x7FFFFFFF;
@@ -358,7 +440,7 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *td
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k)) break;
+    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k, board)) break;
     const U128 q{p * A, __umul64hi(p, A)};
     const U128 u = warp_min_div_res(p, F[w], q, r, target, D[w], lane);
     if (u.lo == 0 && u.hi == 0) continue;
