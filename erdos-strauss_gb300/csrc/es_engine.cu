@@ -506,7 +506,7 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
 }
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 3) k_mark_short(const ShortParams P) {
+__global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
   extern __shared__ __align__(16) u32 tab[];
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (P.hdr->nshort == 0) return;
@@ -773,7 +773,7 @@ __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *
 // ============================================================================ host engine
 
 constexpr int MARK_BLOCK = 128;
-constexpr int SHORT_BLOCK = 256;
+constexpr int SHORT_BLOCK = 384;   // 12 warps: two CTAs of two 37 KB lane tables fill an SM
 
 }  // namespace es
 
@@ -1159,7 +1159,15 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
       sl->h_hdr->nwin = (u32)n;
       sl->h_hdr->nshort = (u32)shortw.size();
       memcpy(sl->h_win, wd.data(), n * sizeof(WinDev));
-      if (!shortw.empty()) memcpy(sl->h_short, shortw.data(), shortw.size() * sizeof(ShortWin));
+      if (!shortw.empty()) {
+        // largest first: the warps of a k_mark_short CTA deal the windows round robin, so the
+        // CTA's last window is a small one
+        std::vector<ShortWin> sorted(shortw);
+        auto work = [](const ShortWin &x) { return (u64)(x.lb - x.la) * (x.lq + 1); };
+        std::stable_sort(sorted.begin(), sorted.end(),
+                         [&](const ShortWin &x, const ShortWin &y) { return work(x) > work(y); });
+        memcpy(sl->h_short, sorted.data(), sorted.size() * sizeof(ShortWin));
+      }
       if (!sl->gexec) { s = capture_graph(e, sl); if (s) return s; }
       CU(cudaGraphLaunch(sl->gexec, sl->stream));
       CU(cudaStreamSynchronize(sl->stream));
