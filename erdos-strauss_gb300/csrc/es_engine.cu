@@ -141,11 +141,11 @@ struct ItemInfo {
 // Per-window residues (lo / M) mod s_d for every distinct stride: computed once per window
 // here, instead of once per (window, lane) item.
 __global__ void k_prep(const BatchHdr *__restrict__ hdr, const WinDev *__restrict__ win,
-                       const u32 *__restrict__ sdist, u32 D, u16 *__restrict__ Qm) {
+                       const u32 *__restrict__ sdist, u32 D, u32 Dq, u16 *__restrict__ Qm) {
   const u64 total = (u64)hdr->nwin * D;
   for (u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (u64)gridDim.x * blockDim.x) {
     const u32 w = (u32)(idx / D), d = (u32)(idx % D);
-    Qm[idx] = (u16)(win[w].Q % sdist[d]);
+    Qm[(size_t)w * Dq + d] = (u16)(win[w].Q % sdist[d]);
   }
 }
 
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
     for (int g = 0; g < (int)GROUP; ++g) ntot += (g < (int)G) ? it.n[g] : 0;
     if (ntot == 0) { __syncthreads(); continue; }
     // segment-start residues of K modulo every distinct stride
-    const u16 *Qm = P.Qm + (size_t)win * P.D;
+    const u16 *Qm = P.Qm + (size_t)win * P.Dq;
     if (G == 1) {
       const u32 b = it.bmask & 1;
       for (u32 d = threadIdx.x; d < P.D; d += BLOCK) {
@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 constexpr int SHORT_LANES = 2;
 constexpr u32 SMD_MAX = 512;       // stride descriptors staged in shared memory
 
+
 __device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFFFFFFu, v); }
 
 // Mask strides [m0, m1) over the segments of SHORT_LANES lanes, in rounds of 32 strides (one
@@ -342,11 +343,39 @@ __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], 
   for (int q = 0; q < SHORT_LANES; ++q)
     #pragma unroll
     for (int c = 0; c < NC; ++c) any |= alive[q][c];
+  u32 kill[SHORT_LANES][NC];
+  // ORs stride k's kill bits into kill: every chunk with one load each in the first round,
+  // only the chunks still alive afterwards
+  auto extract = [&](u32 k, u32 q0, bool first) {
+    const MaskDesc md = mask_desc(smd, mdesc, k);
+    const u32 s = md.s;
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q) {
+      u32 r = q0 + b[q];
+      r = r >= s ? r - s : r;
+      // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
+      const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+      const u32 sh = r & 31;
+      if (first) {
+        u32 w0 = wp[0];
+        #pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const u32 w1 = wp[c + 1];
+          kill[q][c] |= __funnelshift_r(w0, w1, sh);
+          w0 = w1;
+        }
+      } else {
+        #pragma unroll
+        for (int c = 0; c < NC; ++c)
+          if (alive[q][c]) kill[q][c] |= __funnelshift_r(wp[c], wp[c + 1], sh);
+      }
+    }
+  };
   // q0_first: this lane's segment-start residue for stride m0 + lane, loaded by the caller
   // ahead of time; each round loads the next round's while it works
   u32 q0 = q0_first;
-  for (u32 kb = m0; kb < m1 && any; kb += 32) {
-    u32 kill[SHORT_LANES][NC];
+  bool first = true;
+  for (u32 kb = m0; kb < m1 && any;) {
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q)
       #pragma unroll
@@ -354,32 +383,10 @@ __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], 
     const u32 k = kb + lane;
     u32 q0_next = 0;
     if (k + 32 < m1) q0_next = (u32)__ldg(Qrow + mask_desc(smd, mdesc, k + 32).d);
-    if (k < m1) {
-      const MaskDesc md = mask_desc(smd, mdesc, k);
-      const u32 s = md.s;
-      #pragma unroll
-      for (int q = 0; q < SHORT_LANES; ++q) {
-        u32 r = q0 + b[q];
-        r = r >= s ? r - s : r;
-        // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
-        const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
-        const u32 sh = r & 31;
-        if (kb == m0) {                       // first round: every chunk, one load each
-          u32 w0 = wp[0];
-          #pragma unroll
-          for (int c = 0; c < NC; ++c) {
-            const u32 w1 = wp[c + 1];
-            kill[q][c] = __funnelshift_r(w0, w1, sh);
-            w0 = w1;
-          }
-        } else {                              // later rounds: only the chunks still alive
-          #pragma unroll
-          for (int c = 0; c < NC; ++c)
-            if (alive[q][c]) kill[q][c] = __funnelshift_r(wp[c], wp[c + 1], sh);
-        }
-      }
-    }
+    if (k < m1) extract(k, q0, first);
     q0 = q0_next;
+    kb += 32;
+    first = false;
     any = 0;
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q)
@@ -455,13 +462,21 @@ __device__ __forceinline__ u32 short_phase(u32 (&alive)[SHORT_LANES][NC], const 
 
 
 // The segments of SHORT_LANES lanes in one short window, NC 32-position chunks each.
+// The window a warp is marking: its index, and the lane of the warp holding its descriptor
+// (whose q_lo/q_hi registers carry Q = lo / M, read only when there are survivors).
+struct WinRef {
+  u32 wi, q_lo, q_hi;
+  int src;
+};
+
 template <int NC>
 __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *tab, u32 tab_words,
-                                               const MaskDesc *smd, u32 l_first, u32 wi,
-                                               const u64 (&first)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
+                                               const MaskDesc *smd, u32 l_first, const WinRef &R,
+                                               const u64 (&rho)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
                                                const u32 (&b)[SHORT_LANES], const u16 *const (&K0row)[SHORT_LANES],
                                                u32 q0_first, u32 lane) {
-  const u16 *Qrow = P.Qm + (size_t)wi * P.D;
+  const u32 wi = R.wi;
+  const u16 *Qrow = P.Qm + (size_t)wi * P.Dq;
   u32 alive[SHORT_LANES][NC];
   #pragma unroll
   for (int q = 0; q < SHORT_LANES; ++q)
@@ -479,7 +494,11 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
     cnt = short_phase<NC>(alive, P, tab, tab_words, smd, P.nm_cov, P.nm_all, P.nl_cov, P.nl_all, n, b, K0row, Qrow,
                           q0b, lane);
   }
-  if (cnt && lane == 0) {              // survivors are rare: lane 0 writes them in order
+  if (!cnt) return;
+  // survivors are rare: the window's first position index comes from its lane, and lane 0
+  // writes the survivors in order
+  const u64 Q = (u64)__shfl_sync(FULL, R.q_lo, R.src) | ((u64)__shfl_sync(FULL, R.q_hi, R.src) << 32);
+  if (lane == 0) {
     u64 slot = atomicAdd(P.surv_count, (unsigned long long)cnt);
     atomicAdd(&P.cnt[wi].surv, (unsigned long long)cnt);
     #pragma unroll
@@ -493,7 +512,7 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
           if (slot < P.surv_cap) {
             const u64 J = 32 * c + k;
             Surv sv;
-            sv.p = first[q] + P.M * J;
+            sv.p = rho[q] + P.M * (Q + b[q] + J);        // the segment starts at K = Q + b
             sv.J = J;
             sv.win = wi;
             sv.lane = l_first + q;
@@ -533,55 +552,58 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
       rho[q] = P.rho[l];
       K0row[q] = P.K0 + (size_t)l * P.ldk;
     }
-    // Software pipeline over this warp's windows: the descriptor two windows ahead and the
-    // first round's stride residue one window ahead are in flight while a window is marked.
+    // This warp's windows are i = warp + WS t. They are read 32 at a time, one descriptor per
+    // lane in one load, and each lane works out the segments of this CTA's lanes in its window
+    // (positions n and start offset b); a ballot keeps the windows where either lane has a
+    // position and the warp walks those, taking n and b packed in one shuffle. The first
+    // round's stride residue of the next window is loaded while a window is marked.
     constexpr u32 WS = BLOCK / 32;
     const uint4 *sw4 = reinterpret_cast<const uint4 *>(P.shortw);
-    auto load_win = [&](u32 i) {
-      ShortWin W{};
-      if (i < nshort) {
-        const uint4 x = __ldg(sw4 + 2 * (size_t)i), y = __ldg(sw4 + 2 * (size_t)i + 1);
-        W.Q = (u64)x.x | ((u64)x.y << 32);
-        W.lomod = x.z; W.wi = x.w; W.la = y.x; W.lb = y.y; W.lq = y.z; W.lr = y.w;
-      }
-      return W;
-    };
     const u32 d_first = lane < P.nm_cov ? mask_desc(smd, P.mdesc, lane).d : 0u;
-    auto load_q0 = [&](u32 i, const ShortWin &W) {
-      return (i < nshort && lane < P.nm_cov) ? (u32)__ldg(P.Qm + (size_t)W.wi * P.D + d_first) : 0u;
+    auto load_q0 = [&](u32 wi) {
+      return lane < P.nm_cov ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + d_first) : 0u;
     };
-    ShortWin Wn = load_win(warp), Wnn = load_win(warp + WS);
-    u32 q0n = load_q0(warp, Wn);
-    for (u32 i = warp; i < nshort; i += WS) {
-      const ShortWin W = Wn;
-      const u32 q0_first = q0n;
-      Wn = Wnn;
-      Wnn = load_win(i + 2 * WS);
-      q0n = load_q0(i + WS, Wn);
-      u64 first[SHORT_LANES];
-      u32 n[SHORT_LANES], b[SHORT_LANES];
-      u32 nmax = 0;
-      #pragma unroll
-      for (int q = 0; q < SHORT_LANES; ++q) {
-        const u32 l = l0 + q;
-        const u32 r = (u32)rho[q];
-        b[q] = r < W.lomod ? 1u : 0u;
-        const u32 d = r + (b[q] ? (u32)P.M : 0u) - W.lomod;       // (rho - lo) mod M
-        n[q] = (l < P.L && l >= W.la && l < W.lb) ? W.lq + (d < W.lr ? 1u : 0u) : 0u;
-        nmax = max(nmax, n[q]);
+    static_assert(SHORT_LANES == 2 && SEG_SMALL < 512, "n and b of two lanes are packed in one word");
+    for (u32 t0 = 0; warp + WS * t0 < nshort; t0 += 32) {
+      const u32 my = warp + WS * (t0 + lane);
+      uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
+      if (my < nshort) { x = __ldg(sw4 + 2 * (size_t)my); y = __ldg(sw4 + 2 * (size_t)my + 1); }
+      // fields: x = {Q lo, Q hi, lomod, wi}, y = {la, lb, lq, lr}
+      u32 pk = 0;                                  // n0 | n1 << 9 | b0 << 18 | b1 << 19
+      if (my < nshort) {
+        #pragma unroll
+        for (int q = 0; q < SHORT_LANES; ++q) {
+          const u32 l = l0 + q;
+          const u32 r = (u32)rho[q];
+          const u32 bq = r < x.z ? 1u : 0u;
+          const u32 d = r + (bq ? (u32)P.M : 0u) - x.z;              // (rho - lo) mod M
+          const u32 nq = (l < P.L && l >= y.x && l < y.y) ? y.z + (d < y.w ? 1u : 0u) : 0u;
+          pk |= (nq << (9 * q)) | (bq << (18 + q));
+        }
       }
-      if (nmax == 0) continue;
-      #pragma unroll
-      for (int q = 0; q < SHORT_LANES; ++q) first[q] = rho[q] + P.M * (W.Q + b[q]);
-      switch ((nmax + 31) >> 5) {
-        case 1: short_segments<1>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 2: short_segments<2>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 3: short_segments<3>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 4: short_segments<4>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 5: short_segments<5>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 6: short_segments<6>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        case 7: short_segments<7>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
-        default: short_segments<8>(P, tab, tab_words, smd, l0, W.wi, first, n, b, K0row, q0_first, lane); break;
+      unsigned todo = __ballot_sync(FULL, (pk & 0x3FFFFu) != 0);
+      u32 q0n = todo ? load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1)) : 0u;
+      while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const u32 pj = __shfl_sync(FULL, pk, j);
+        const u32 wi = __shfl_sync(FULL, x.w, j);
+        const u32 q0_first = q0n;
+        if (todo) q0n = load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1));
+        const u32 n[SHORT_LANES] = {pj & 511u, (pj >> 9) & 511u};
+        const u32 b[SHORT_LANES] = {(pj >> 18) & 1u, (pj >> 19) & 1u};
+        const u32 nmax = max(n[0], n[1]);
+        const WinRef R{wi, x.x, x.y, j};
+        switch ((nmax + 31) >> 5) {
+          case 1: short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 2: short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 3: short_segments<3>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 4: short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 5: short_segments<5>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 6: short_segments<6>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          case 7: short_segments<7>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+          default: short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
+        }
       }
     }
     __syncthreads();
@@ -773,7 +795,10 @@ __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *
 // ============================================================================ host engine
 
 constexpr int MARK_BLOCK = 128;
-constexpr int SHORT_BLOCK = 384;   // 12 warps: two CTAs of two 37 KB lane tables fill an SM
+#ifndef ES_SHORT_BLOCK
+#define ES_SHORT_BLOCK 512
+#endif
+constexpr int SHORT_BLOCK = ES_SHORT_BLOCK;   // 16 warps, 64 registers: two CTAs of two 37 KB lane tables fill an SM
 
 }  // namespace es
 
@@ -837,7 +862,7 @@ struct es_engine {
   size_t ncov = 0;
   // marking order: filters sorted by stride within each phase
   std::vector<uint32_t> order;
-  uint32_t nf = 0, ldk = 0, D = 0, Lpad = 0;
+  uint32_t nf = 0, ldk = 0, D = 0, Dq = 0, Lpad = 0;
   int device = 0, sm_count = 0, mark_occupancy = 0;
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
@@ -906,12 +931,12 @@ static es_status ensure_capacity(es_engine *e, Slot *sl, size_t nwin, size_t cap
     CU(cudaMalloc(&sl->d_win, want * sizeof(WinDev)));
     CU(cudaMalloc(&sl->d_cnt, want * sizeof(WinCount)));
     CU(cudaMalloc(&sl->d_shortw, want * sizeof(ShortWin)));
-    CU(cudaMalloc(&sl->d_Qm, want * std::max<u32>(e->D, 1) * sizeof(u16)));
+    CU(cudaMalloc(&sl->d_Qm, want * std::max<u32>(e->Dq, 8) * sizeof(u16)));
     CU(cudaMallocHost(&sl->h_win, want * sizeof(WinDev)));
     CU(cudaMallocHost(&sl->h_short, want * sizeof(ShortWin)));
     CU(cudaMallocHost(&sl->h_cnt, want * sizeof(WinCount)));
     sl->win_cap = sl->shortw_cap = want;
-    sl->qm_cap = want * std::max<u32>(e->D, 1);
+    sl->qm_cap = want * std::max<u32>(e->Dq, 8);
   }
   if (cap > sl->cap) {
     drop_graph(sl);
@@ -937,7 +962,7 @@ static MarkParams mark_params(const es_engine *e, const Slot *sl) {
   P.surv = sl->d_surv; P.surv_count = sl->d_ctr + 1; P.cnt = sl->d_cnt;
   P.hdr = sl->d_hdr; P.surv_cap = sl->cap; P.M = e->M;
   P.L = (u32)e->classes.size(); P.ldk = e->ldk; P.nf = e->nf; P.ncov = (u32)e->ncov;
-  P.D = e->D;
+  P.D = e->D; P.Dq = e->Dq;
   P.r_bytes = (4 * e->D + 15) & ~15u;
   return P;
 }
@@ -1034,7 +1059,7 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
   CU(cudaMemcpyAsync(sl->d_win, sl->h_win, ncopy * sizeof(WinDev), cudaMemcpyHostToDevice, st));
   if (nshort_copy) CU(cudaMemcpyAsync(sl->d_shortw, sl->h_short, nshort_copy * sizeof(ShortWin), cudaMemcpyHostToDevice, st));
   CU(rec(0));
-  k_prep<<<e->sm_count * 4, 256, 0, st>>>(sl->d_hdr, sl->d_win, e->d_sdist, e->D, sl->d_Qm);
+  k_prep<<<e->sm_count * 4, 256, 0, st>>>(sl->d_hdr, sl->d_win, e->d_sdist, e->D, e->Dq, sl->d_Qm);
   CU(cudaGetLastError());
   CU(rec(7));
   {
@@ -1042,7 +1067,7 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
     S.rho = e->d_rho; S.K0 = e->d_K0; S.fdesc = e->d_fdesc; S.Qm = sl->d_Qm; S.mtab = e->d_mtab;
     S.mdesc = e->d_mdesc; S.lfil = e->d_lfil; S.win = sl->d_win; S.shortw = sl->d_shortw;
     S.surv = sl->d_surv; S.surv_count = sl->d_ctr + 1; S.cnt = cnt; S.surv_cap = sl->cap; S.M = e->M;
-    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Wpad = e->Wpad; S.hdr = sl->d_hdr;
+    S.L = (u32)e->classes.size(); S.ldk = e->ldk; S.D = e->D; S.Dq = e->Dq; S.Wpad = e->Wpad; S.hdr = sl->d_hdr;
     S.nm_cov = e->nm_cov; S.nm_all = e->nm_all; S.nl_cov = e->nl_cov; S.nl_all = e->nl_all;
     k_mark_short<SHORT_BLOCK><<<(S.L + SHORT_LANES - 1) / SHORT_LANES, SHORT_BLOCK, short_smem(e), st>>>(S);
     CU(cudaGetLastError());
@@ -1270,6 +1295,7 @@ static es_status build_tables(es_engine *e) {
   sd.erase(std::unique(sd.begin(), sd.end()), sd.end());
   if (sd.size() > (size_t)DMAX) return fail(e, ES_ERR_ARG, "more than 8192 distinct filter strides");
   e->D = (u32)sd.size();
+  e->Dq = (e->D + 7) & ~7u;                        // Qm rows: whole 16-byte chunks
   std::vector<u64> om(nf), orr(nf);
   std::vector<u32> og(nf), oinv(nf), fdesc(nf);
   for (size_t k = 0; k < nf; ++k) {
@@ -1431,7 +1457,7 @@ static u64 request_bytes(const es_engine *e, const es_window *w, size_t n) {
   u64 pos = 0;
   for (size_t i = 0; i < n; ++i) pos += positions_in(e, w[i].lo, w[i].hi);
   const u64 surv = std::min<u64>(std::max<u64>(pos / 64, 1024), 1ull << 26);
-  return n * (sizeof(WinDev) + sizeof(ShortWin) + sizeof(WinCount) + 2ull * e->D) +
+  return n * (sizeof(WinDev) + sizeof(ShortWin) + sizeof(WinCount) + 2ull * e->Dq) +
          surv * (sizeof(Surv) + 3 * sizeof(u32) + sizeof(RecDev));
 }
 

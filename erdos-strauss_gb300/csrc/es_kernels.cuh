@@ -63,7 +63,7 @@ struct MarkParams {
   const u16 *K0T;          // [nf][Lpad] the same table, lane-contiguous (16-lane vector loads)
   const u32 *fdesc;        // [nf] stride s (low 16 bits) | index of s among distinct strides
   const u32 *sdist;        // [D] distinct strides
-  const u16 *Qm;           // [nwin][D] (lo / M) mod s_d per window
+  const u16 *Qm;           // [nwin][Dq] (lo / M) mod s_d per window (rows of Dq >= D, 16-byte multiples)
   const WinDev *win;       // [nwin]
   u64 *queue;              // work-queue head (persistent schedule)
   Surv *surv;              // survivor list
@@ -72,7 +72,7 @@ struct MarkParams {
   const BatchHdr *hdr;     // total_items, nwin
   u64 surv_cap;
   u64 M;
-  u32 L, Lpad, ldk, nf, ncov, D;
+  u32 L, Lpad, ldk, nf, ncov, D, Dq;
   u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
 };
 
@@ -97,7 +97,7 @@ struct ShortParams {
   const u32 *rho;
   const u16 *K0;
   const u32 *fdesc;
-  const u16 *Qm;            // [nwin][D]
+  const u16 *Qm;            // [nwin][Dq]
   const u64 *mtab;          // [L][Wpad] kill masks
   const MaskDesc *mdesc;    // covers' mask strides [0, nm_cov), then stage B' [nm_cov, nm_all)
   const u32 *lfil;          // filters not covered by a mask: covers [0, nl_cov), then B' [nl_cov, nl_all)
@@ -108,7 +108,7 @@ struct ShortParams {
   WinCount *cnt;
   u64 surv_cap, M;
   const BatchHdr *hdr;      // nshort
-  u32 L, ldk, D, Wpad, nm_cov, nm_all, nl_cov, nl_all;
+  u32 L, ldk, D, Dq, Wpad, nm_cov, nm_all, nl_cov, nl_all;
 };
 
 struct HardSlot;
