@@ -6,7 +6,8 @@ floor(2^(16 + 12 U)) and log-uniform start heights over [255255, 1.8446744065e19
 splitmix64 (erdos-strauss_gb300/workloads.py), wheel 2042040, the pruned gpu filter table.
 One step = one pass of the whole funnel (marking, compaction, Miller-Rabin, rung walk, direct
 search) over every window of the batch, through es_run_batch with the persistent schedule,
-records and counters returned to the host.
+records and counters returned to the host. Before the warm-up, es_autotune picks the kernel
+schedule on the same batch (untimed; every schedule gives identical results).
 
   value   integers of the batch / device time of the step's kernels (CUDA events on the
           engine's stream, inputs already resident; L2 flushed before every timed step)
@@ -54,6 +55,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve", type=int, default=2000, help="serving requests (0: no serving leg)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule")
     return ap.parse_args()
 
 
@@ -343,6 +345,7 @@ def run_gpu(args, ws, rank, local):
     eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local)
     wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
     n_int = integers(wins)
+    schedule = eng.autotune(wins, repeats=2) if not args.no_autotune else eng.schedule()
     for _ in range(args.warmup):
         eng.run_batch(wins)
     barrier(ws)
@@ -421,7 +424,8 @@ def run_gpu(args, ws, rank, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
                 "config": {"workload": "batch4096", "windows": args.windows, "integers_per_step": n_int,
                            "wheel": 2042040, "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED,
-                           "schedule": "persistent", "l2": flush_note, "parallelism": "replicas x%d" % ws},
+                           "schedule": "persistent", "kernel_schedule": schedule, "l2": flush_note,
+                           "parallelism": "replicas x%d" % ws},
                 # copied every step: batch header, window and short-window descriptors in; run
                 # counters, status, per-window counters and records out (pinned staging)
                 "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),

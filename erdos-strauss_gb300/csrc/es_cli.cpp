@@ -6,7 +6,8 @@
 //                    [--no-rung]   (cover_scan's test hook: skip stage D, exercise stage E)
 //   rung_scan3_gb300 --verify | --dump-classes [--wheel M] | --check-direct LO N
 //                    | --check-factor [N]
-// plus options of its own: --device N, --profile (stage timings on stderr), and
+// plus options of its own: --device N, --profile (stage timings on stderr), --autotune (time
+// the engine's candidate schedules on the windows first and keep the fastest), and
 //   rung_scan3_gb300 --batch FILE [flags]   one "LO HI" per line, each window's stream and
 //                                           SUMMARY in file order, run as one batch.
 // stdout carries only the certificate stream and SUMMARY; everything else goes to stderr.
@@ -191,7 +192,7 @@ int main(int argc, char **argv) {
     fprintf(stderr,
             "usage: %s LO HI [--mmax N] [--wheel M] [--seg N] [--threads N]\n"
             "                 [--shard i/n] [--progress N] [--filters FILE] [--sieve P]\n"
-            "                 [--no-emit-survivors] [--device N] [--profile]\n"
+            "                 [--no-emit-survivors] [--device N] [--profile] [--autotune]\n"
             "       %s --batch FILE [flags]\n"
             "       %s --verify | --dump-classes [--wheel M] | --check-direct LO N | --check-factor [N]\n"
             "GB300 verification sieve: certifies 4/p solvable for every prime in [LO, HI),\n"
@@ -202,7 +203,7 @@ int main(int argc, char **argv) {
   u64 lo = 0, hi = 0;
   if (!batch) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
   u64 M = 2042040, mmax = 10000, seg = 262144, shard = 0, nshard = 1, sieve_p = 0;
-  bool emit_surv = true, profile = false, no_rung = false;
+  bool emit_surv = true, profile = false, no_rung = false, autotune = false;
   const char *ffile = nullptr;
   for (int i = 3; i < argc; ++i) {
     if (!strcmp(argv[i], "--mmax") && i + 1 < argc) mmax = strtoull(argv[++i], 0, 10);
@@ -219,6 +220,7 @@ int main(int argc, char **argv) {
     } else if (!strcmp(argv[i], "--no-emit-survivors")) emit_surv = false;
     else if (!strcmp(argv[i], "--profile")) profile = true;
     else if (!strcmp(argv[i], "--no-rung")) no_rung = true;
+    else if (!strcmp(argv[i], "--autotune")) autotune = true;
     else { fprintf(stderr, "FATAL: unknown option '%s'\n", argv[i]); return 1; }
   }
   if (!seg) seg = 262144;
@@ -285,6 +287,17 @@ int main(int argc, char **argv) {
           (unsigned long long)info.wheel_pmin, (unsigned long long)info.n_certified,
           (unsigned long long)info.filter_fnv64, ffile ? ffile : "generated", (unsigned long long)sieve_p,
           (unsigned long long)(info.n_filters - info.n_certified));
+  if (autotune) {
+    es_schedule sc;
+    const es_status a = es_autotune(e, wins.data(), wins.size(), 2, &sc);
+    if (a != ES_OK) {
+      fprintf(stderr, "FATAL: autotune: %s: %s\n", es_status_str(a), es_last_error(e));
+      es_close(e);
+      return 1;
+    }
+    fprintf(stderr, "[rung_scan3_gb300] autotune: short_max=%u rung_blocks_per_sm=%u\n", sc.short_max,
+            sc.rung_blocks_per_sm);
+  }
   const auto t1 = std::chrono::steady_clock::now();
   std::vector<es_counters> cnt(wins.size());
   es_records recs{};

@@ -863,6 +863,7 @@ struct es_engine {
   // marking order: filters sorted by stride within each phase
   std::vector<uint32_t> order;
   uint32_t nf = 0, ldk = 0, D = 0, Dq = 0, Lpad = 0;
+  es_schedule sched{es::SEG_SMALL, 6, {0, 0, 0, 0, 0, 0}};   // es_set_schedule / es_autotune
   int device = 0, sm_count = 0, mark_occupancy = 0;
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
@@ -1007,7 +1008,7 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
     const u64 maxpos = len ? (len - 1) / M + 1 : 0;     // most positions any lane can hold
     d.item0 = items;
     d.G = 1; d.lane0 = 0;
-    if (maxpos <= SEG_SMALL) {
+    if (maxpos <= e->sched.short_max) {
       d.seg = SEG_SMALL; d.nseg = 0; d.groups = 0;
       if (maxpos) {
         // Shorter than M: only the classes in [lo mod M, lo mod M + len) have a position,
@@ -1083,7 +1084,7 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
   k_mr2<<<e->sm_count * 2, 256, 0, st>>>(T);
   CU(cudaGetLastError());
   CU(rec(2));
-  k_rung<<<e->sm_count * 6, RUNG_WARPS * 32, 0, st>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
+  k_rung<<<e->sm_count * e->sched.rung_blocks_per_sm, RUNG_WARPS * 32, 0, st>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
   CU(cudaGetLastError());
   CU(rec(3));
   k_direct<<<e->sm_count, 32, 0, st>>>(T);
@@ -1774,6 +1775,74 @@ size_t es_format_summary(const es_engine *e, uint64_t lo, uint64_t hi, const es_
                          (unsigned long long)c->rung, (unsigned long long)c->direct,
                          (unsigned long long)c->survivors);
   return (k > 0 && (size_t)k < cap) ? (size_t)k : 0;
+}
+
+es_status es_get_schedule(const es_engine *e, es_schedule *o) {
+  if (!e || !o) return ES_ERR_ARG;
+  *o = e->sched;
+  return ES_OK;
+}
+
+es_status es_set_schedule(es_engine *e, const es_schedule *s) {
+  if (!e || !s) return ES_ERR_ARG;
+  if (s->short_max < 1 || s->short_max > es::SEG_SMALL) return fail(e, ES_ERR_ARG, "short_max must be in 1..256");
+  if (s->rung_blocks_per_sm < 1 || s->rung_blocks_per_sm > 16)
+    return fail(e, ES_ERR_ARG, "rung_blocks_per_sm must be in 1..16");
+  for (uint32_t r : s->reserved)
+    if (r) return fail(e, ES_ERR_ARG, "reserved schedule fields must be zero");
+  // every slot idle while the schedule changes; their graphs hold the old launch shapes
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (Slot &sl : e->slots) locks.emplace_back(sl.mu);
+  cudaSetDevice(e->device);
+  e->sched = *s;
+  for (Slot &sl : e->slots) drop_graph(&sl);
+  return ES_OK;
+}
+
+es_status es_autotune(es_engine *e, const es_window *w, size_t n, int repeats, es_schedule *chosen) {
+  if (!e || !w || n == 0 || repeats < 1 || repeats > 1000) return ES_ERR_ARG;
+  static const uint32_t SHORT[] = {64, 128, 256};
+  static const uint32_t RUNG[] = {4, 6, 8};
+  const es_schedule before = e->sched;
+  std::vector<es_counters> base(n), cur(n);
+  es_records rbase{nullptr, 0};
+  es_schedule best = before;
+  double best_ms = 1e300;
+  bool first = true;
+  es_status st = ES_OK;
+  for (uint32_t sm : SHORT) {
+    for (uint32_t rb : RUNG) {
+      es_schedule c = before;
+      c.short_max = sm;
+      c.rung_blocks_per_sm = rb;
+      if ((st = es_set_schedule(e, &c)) != ES_OK) break;
+      double ms = 1e300;
+      for (int r = 0; r <= repeats && st == ES_OK; ++r) {
+        es_records rc{nullptr, 0};
+        st = es_run_batch(e, w, n, ES_SCHED_PERSISTENT, cur.data(), &rc);
+        if (st != ES_OK) break;
+        if (first) {                               // the first run defines the results
+          base = cur;
+          rbase = rc;
+          first = false;
+          continue;
+        }
+        const bool same = memcmp(cur.data(), base.data(), n * sizeof(es_counters)) == 0 && rc.n == rbase.n &&
+                          (rc.n == 0 || memcmp(rc.recs, rbase.recs, rc.n * sizeof(es_record)) == 0);
+        es_free_records(&rc);
+        if (!same) st = fail(e, ES_ERR_DEVICE_STATUS, "autotune: a schedule changed a result");
+        if (r > 0) ms = std::min(ms, e->slots[0].timing.total_ms);   // run 0 warms up (graph capture)
+      }
+      if (st != ES_OK) break;
+      if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    if (st != ES_OK) break;
+  }
+  es_free_records(&rbase);
+  if (st != ES_OK) { es_set_schedule(e, &before); return st; }
+  st = es_set_schedule(e, &best);
+  if (st == ES_OK && chosen) *chosen = best;
+  return st;
 }
 
 es_status es_info(const es_engine *e, es_info_t *o) {

@@ -112,7 +112,13 @@ __device__ __forceinline__ bool cancelled(const volatile int *cancel, int my_k) 
 // board only speeds things up: the owner checks every divisor it is handed (1 < d < n,
 // n mod d == 0) and its own walks still finish the job alone. No warp ever waits for another.
 constexpr u32 HARD_SLOTS = 32;                 // one per lane of a scanning warp
-constexpr u64 RHO_POST_STEPS = 1024;           // steps per lane before a cofactor is posted
+#ifndef ES_RHO_POST_STEPS
+#define ES_RHO_POST_STEPS 1024
+#endif
+#ifndef ES_HELP_SLEEP_NS
+#define ES_HELP_SLEEP_NS 2000
+#endif
+constexpr u64 RHO_POST_STEPS = ES_RHO_POST_STEPS;  // steps per lane before a cofactor is posted
 constexpr u64 HELP_STEPS = 1ull << 16;         // steps per lane of one helping session
 constexpr u32 HELP_IDLE_POLLS = 4096;          // empty-board polls (2 us apart) before a helper leaves
 constexpr u32 HELP_MAX_ROUNDS = 1024;          // board scans (sessions or polls) per helper, at most
@@ -228,7 +234,7 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
     const unsigned posted = __ballot_sync(FULL, st == 2u);
     if (!posted) {
       ++idle;
-      __nanosleep(2000);
+      __nanosleep(ES_HELP_SLEEP_NS);
       continue;
     }
     u64 ses = 0;

@@ -69,6 +69,13 @@ class Info(C.Structure):
                [("pinned", C.c_int), ("classes_sha256", C.c_char * 72)]
 
 
+class Schedule(C.Structure):
+    _fields_ = [("short_max", C.c_uint32), ("rung_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+
+    def as_dict(self):
+        return {"short_max": int(self.short_max), "rung_blocks_per_sm": int(self.rung_blocks_per_sm)}
+
+
 class Timing(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_ms", "mark_ms", "mr_ms", "rung_ms", "direct_ms", "prep_ms",
                                           "mark_short_ms", "mark_long_ms")] + \
@@ -102,6 +109,9 @@ def load_library(path=LIB_PATH):
         "es_format_record": (C.c_size_t, [P(Record), C.c_char_p, C.c_size_t]),
         "es_format_summary": (C.c_size_t, [e, C.c_uint64, C.c_uint64, P(Counters), C.c_char_p, C.c_size_t]),
         "es_info": (C.c_int, [e, P(Info)]),
+        "es_get_schedule": (C.c_int, [e, P(Schedule)]),
+        "es_set_schedule": (C.c_int, [e, P(Schedule)]),
+        "es_autotune": (C.c_int, [e, P(Window), C.c_size_t, C.c_int, P(Schedule)]),
         "es_classes": (C.c_int, [e, P(C.c_uint64), C.c_size_t]),
         "es_timing": (C.c_int, [e, P(Timing)]),
         "es_status_str": (C.c_char_p, [C.c_int]),
@@ -249,6 +259,29 @@ class Engine:
         nrec = r.n
         self.lib.es_free_records(C.byref(r))
         return nrec
+
+    # ------------------------------------------------------------------ schedule
+    def schedule(self):
+        sc = Schedule()
+        self._check(self.lib.es_get_schedule(self.h, C.byref(sc)))
+        return sc.as_dict()
+
+    def set_schedule(self, short_max=None, rung_blocks_per_sm=None):
+        sc = Schedule()
+        self._check(self.lib.es_get_schedule(self.h, C.byref(sc)))
+        if short_max is not None:
+            sc.short_max = short_max
+        if rung_blocks_per_sm is not None:
+            sc.rung_blocks_per_sm = rung_blocks_per_sm
+        self._check(self.lib.es_set_schedule(self.h, C.byref(sc)))
+
+    def autotune(self, windows, repeats=2):
+        """Time the candidate schedules on these windows, keep the fastest; returns it."""
+        n = len(windows)
+        w = (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        sc = Schedule()
+        self._check(self.lib.es_autotune(self.h, w, n, repeats, C.byref(sc)))
+        return sc.as_dict()
 
     # ------------------------------------------------------------------ serving
     def submit(self, windows):

@@ -173,6 +173,27 @@ size_t es_format_record(const es_record *r, char *buf, size_t cap);
 size_t es_format_summary(const es_engine *engine, uint64_t lo, uint64_t hi, const es_counters *c,
                          char *buf, size_t cap);
 
+/* Run-time schedule of the engine's kernels. Every schedule gives the same counters and
+ * records; only the time differs. No reference counterpart (the reference's CPU loop has
+ * nothing to schedule). */
+typedef struct {
+  uint32_t short_max;            /* windows whose lanes hold at most this many positions (1..256)
+                                    are marked by the short-window kernel, longer ones by the
+                                    segment marking; default 256 */
+  uint32_t rung_blocks_per_sm;   /* stage-D grid in blocks per SM (1..16); default 6 */
+  uint32_t reserved[6];          /* zero */
+} es_schedule;
+
+es_status es_get_schedule(const es_engine *engine, es_schedule *out);
+/* ES_ERR_ARG for a value out of range; captured batch graphs are rebuilt on the next run. */
+es_status es_set_schedule(es_engine *engine, const es_schedule *s);
+/* Autotuner: runs the windows (persistent schedule) under each candidate schedule -- short_max
+ * in {64, 128, 256} x rung_blocks_per_sm in {4, 6, 8} -- once to warm up and `repeats` times
+ * timed, keeps the best device time of each, checks that every candidate gave identical
+ * counters and records (ES_ERR_DEVICE_STATUS if not), and sets the fastest. `chosen` may be
+ * null. */
+es_status es_autotune(es_engine *engine, const es_window *w, size_t n, int repeats, es_schedule *chosen);
+
 es_status es_info(const es_engine *engine, es_info_t *out);
 /* The wheel classes in lane order (build_wheel, sieve/rung_scan3.cpp:211-226). */
 es_status es_classes(const es_engine *engine, uint64_t *out, size_t cap);
