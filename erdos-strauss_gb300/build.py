@@ -48,15 +48,16 @@ def build(verbose=False, ptxas_info=False):
         "es_engine.o": [nvcc] + NVFLAGS + extra + ["-c", os.path.join(CSRC, "es_engine.cu"), "-o"],
         "es_noalloc.o": [nvcc] + NVFLAGS + extra + ["-c", os.path.join(CSRC, "es_noalloc.cu"), "-o"],
         "es_wheel.o": ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "es_wheel.cpp"), "-o"],
+        "es_digest.o": ["g++"] + CXXFLAGS + ["-O3", "-c", os.path.join(CSRC, "es_digest.cpp"), "-o"],
         "es_cli.o": ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "es_cli.cpp"), "-o"],
     }
     logs = []
-    with ThreadPoolExecutor(max_workers=4) as ex:
+    with ThreadPoolExecutor(max_workers=5) as ex:
         futs = [ex.submit(_run, cmd + [os.path.join(BUILD, o)]) for o, cmd in objs.items()]
         for f in futs:
             logs.append(f.result())
     _run([nvcc] + ARCH + ["-shared", "-o", LIB, os.path.join(BUILD, "es_engine.o"), os.path.join(BUILD, "es_noalloc.o"),
-                          os.path.join(BUILD, "es_wheel.o")])
+                          os.path.join(BUILD, "es_wheel.o"), os.path.join(BUILD, "es_digest.o")])
     _run(["g++", "-o", CLI, os.path.join(BUILD, "es_cli.o"), "-L" + HERE, "-les_sieve", "-Wl,-rpath,$ORIGIN"])
     if verbose or ptxas_info:
         sys.stdout.write("".join(logs))

@@ -7,16 +7,28 @@
 //   rung_scan3_gb300 --verify | --dump-classes [--wheel M] | --check-direct LO N
 //                    | --check-factor [N]
 // plus options of its own: --device N, --profile (stage timings on stderr), --autotune (time
-// the engine's candidate schedules on the windows first and keep the fastest), and
+// the engine's candidate schedules on the windows first and keep the fastest),
+//   --meta FILE [--order round|lane] [--chunk-rounds R]
+//                      the shard record of tools/run19.sh:70-77 instead of the stream: the
+//                      stream is hashed as it is produced (certs=, cert_sha256=), SURVIVOR
+//                      lines kept verbatim, SUMMARY last; stdout gets the SUMMARY only.
+//                      --order round (default) emits the production driver's order
+//                      (sieve/cuda/scan.cu:266-310: rounds of --seg positions, lanes in wheel
+//                      order within a round), running the shard in chunks of R rounds (default
+//                      64) so no chunk holds more than its own records; --order lane emits
+//                      rung_scan3's order and runs the shard as one window. And
 //   rung_scan3_gb300 --batch FILE [flags]   one "LO HI" per line, each window's stream and
 //                                           SUMMARY in file order, run as one batch.
 // stdout carries only the certificate stream and SUMMARY; everything else goes to stderr.
 // Exit status: 0 no survivors, 2 survivors present, 1 refusal or error.
 #include "../../include/es_sieve.h"
+#include "es_digest.h"
 #include "es_wheel.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cinttypes>
+#include <ctime>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -173,6 +185,82 @@ static int self_test(int device) {
   return fails ? 1 : 0;
 }
 
+static std::string file_sha256(const char *path) {
+  FILE *f = path ? fopen(path, "rb") : nullptr;
+  if (!f) return "none";
+  es::Sha256 h;
+  std::vector<char> buf(1 << 16);
+  size_t k;
+  while ((k = fread(buf.data(), 1, buf.size(), f)) > 0) h.update(buf.data(), k);
+  fclose(f);
+  return h.hex();
+}
+
+// The shard record of tools/run19.sh:70-77 for [lo, hi): the stream is formatted and hashed
+// chunk by chunk, never stored. Round order (sieve/cuda/scan.cu:266-310) needs each chunk to
+// start on a round boundary of every lane: chunks are whole multiples of M * seg integers, so
+// lane l's first position moves by exactly chunk_rounds * seg positions from one chunk to the
+// next, and sorting a chunk's lane-major records by J / seg (stably) gives round, lane, J.
+static int write_meta(es_engine *e, const char *path, u64 lo, u64 hi, u64 M, u64 seg, u64 chunk_rounds,
+                      bool round_order, bool emit_surv, u64 shard, u64 nshard, const char *ffile, const char *threads,
+                      std::chrono::steady_clock::time_point t0) {
+  es::Sha256 h;
+  u64 certs = 0;
+  std::string surv_lines;
+  es_counters tot{};
+  const unsigned __int128 span128 = (unsigned __int128)M * seg * chunk_rounds;
+  const u64 span = round_order && span128 < (unsigned __int128)(hi - lo) ? (u64)span128 : hi - lo;
+  std::string chunk_text;
+  char line[160];
+  for (u64 a = lo; a < hi || (a == lo && lo == hi);) {
+    const u64 b = hi - a > span ? a + span : hi;
+    es_counters c;
+    es_records r{};
+    const es_status s = es_run_window(e, a, b, &c, &r);
+    if (s != ES_OK) {
+      fprintf(stderr, "FATAL: %s: %s\n", es_status_str(s), es_last_error(e));
+      return 1;
+    }
+    tot.positions += c.positions; tot.covered += c.covered; tot.sieved += c.sieved; tot.mr += c.mr;
+    tot.composite += c.composite; tot.rung += c.rung; tot.direct += c.direct; tot.survivors += c.survivors;
+    if (round_order) std::stable_sort(r.recs, r.recs + r.n, [&](const es_record &x, const es_record &y) {
+      return x.J / seg < y.J / seg;
+    });
+    chunk_text.clear();
+    for (size_t i = 0; i < r.n; ++i) {
+      if (!emit_surv && r.recs[i].kind == ES_REC_SURVIVOR) continue;
+      const size_t k = es_format_record(&r.recs[i], line, sizeof line);
+      chunk_text.append(line, k);
+      if (r.recs[i].kind == ES_REC_SURVIVOR) surv_lines.append(line, k);
+      else ++certs;
+    }
+    h.update(chunk_text);
+    es_free_records(&r);
+    if (b == hi) break;
+    a = b;
+  }
+  char summary[512];
+  if (!es_format_summary(e, lo, hi, &tot, summary, sizeof summary)) { fprintf(stderr, "FATAL: SUMMARY\n"); return 1; }
+  const int rc = tot.survivors ? 2 : 0;
+  const long wall = (long)std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  char date[32];
+  const time_t now = time(nullptr);
+  strftime(date, sizeof date, "%Y-%m-%d %H:%M:%S", gmtime(&now));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE *f = fopen(tmp.c_str(), "w");
+  if (!f) { fprintf(stderr, "FATAL: cannot write %s\n", tmp.c_str()); return 1; }
+  fprintf(f, "# shard %llu/%llu  rc=%d  wall=%lds  attempt=1  %s\n", (unsigned long long)shard,
+          (unsigned long long)nshard, rc, wall, date);
+  fprintf(f, "# binary_commit=gb300 table_sha256=%s threads=%s order=%s\n", file_sha256(ffile).c_str(), threads,
+          round_order ? "round" : "lane");
+  fprintf(f, "certs=%llu\ncert_sha256=%s\n", (unsigned long long)certs, h.hex().c_str());
+  fputs(surv_lines.c_str(), f);
+  fputs(summary, f);                                   // last: its presence marks the meta complete
+  if (fclose(f) != 0 || rename(tmp.c_str(), path) != 0) { fprintf(stderr, "FATAL: cannot write %s\n", path); return 1; }
+  fputs(summary, stdout);
+  return rc;
+}
+
 int main(int argc, char **argv) {
   int device = 0;
   for (int i = 1; i + 1 < argc; ++i) if (!strcmp(argv[i], "--device")) device = atoi(argv[i + 1]);
@@ -193,6 +281,7 @@ int main(int argc, char **argv) {
             "usage: %s LO HI [--mmax N] [--wheel M] [--seg N] [--threads N]\n"
             "                 [--shard i/n] [--progress N] [--filters FILE] [--sieve P]\n"
             "                 [--no-emit-survivors] [--device N] [--profile] [--autotune]\n"
+            "                 [--meta FILE [--order round|lane] [--chunk-rounds R]]\n"
             "       %s --batch FILE [flags]\n"
             "       %s --verify | --dump-classes [--wheel M] | --check-direct LO N | --check-factor [N]\n"
             "GB300 verification sieve: certifies 4/p solvable for every prime in [LO, HI),\n"
@@ -203,14 +292,15 @@ int main(int argc, char **argv) {
   u64 lo = 0, hi = 0;
   if (!batch) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
   u64 M = 2042040, mmax = 10000, seg = 262144, shard = 0, nshard = 1, sieve_p = 0;
-  bool emit_surv = true, profile = false, no_rung = false, autotune = false;
-  const char *ffile = nullptr;
+  bool emit_surv = true, profile = false, no_rung = false, autotune = false, round_order = true;
+  const char *ffile = nullptr, *meta = nullptr, *threads = "1";
+  u64 chunk_rounds = 64;
   for (int i = 3; i < argc; ++i) {
     if (!strcmp(argv[i], "--mmax") && i + 1 < argc) mmax = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--wheel") && i + 1 < argc) M = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--seg") && i + 1 < argc) seg = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--progress") && i + 1 < argc) ++i;
-    else if (!strcmp(argv[i], "--threads") && i + 1 < argc) ++i;
+    else if (!strcmp(argv[i], "--threads") && i + 1 < argc) threads = argv[++i];
     else if (!strcmp(argv[i], "--device") && i + 1 < argc) ++i;
     else if (!strcmp(argv[i], "--filters") && i + 1 < argc) ffile = argv[++i];
     else if (!strcmp(argv[i], "--sieve") && i + 1 < argc) sieve_p = strtoull(argv[++i], 0, 10);
@@ -221,10 +311,20 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[i], "--profile")) profile = true;
     else if (!strcmp(argv[i], "--no-rung")) no_rung = true;
     else if (!strcmp(argv[i], "--autotune")) autotune = true;
+    else if (!strcmp(argv[i], "--meta") && i + 1 < argc) meta = argv[++i];
+    else if (!strcmp(argv[i], "--chunk-rounds") && i + 1 < argc) chunk_rounds = strtoull(argv[++i], 0, 10);
+    else if (!strcmp(argv[i], "--order") && i + 1 < argc) {
+      const char *o = argv[++i];
+      if (!strcmp(o, "round")) round_order = true;
+      else if (!strcmp(o, "lane")) round_order = false;
+      else { fprintf(stderr, "FATAL: --order must be round or lane\n"); return 1; }
+    }
     else { fprintf(stderr, "FATAL: unknown option '%s'\n", argv[i]); return 1; }
   }
   if (!seg) seg = 262144;
   if (nshard == 0) nshard = 1;
+  if (!chunk_rounds) chunk_rounds = 64;
+  if (meta && batch) { fprintf(stderr, "FATAL: --meta writes one shard's record; it does not take --batch\n"); return 1; }
   if (!batch && nshard > 1) {                 // ceil-span tiling, sieve/rung_scan3.cpp:1022-1027
     const u64 span = (hi - lo + nshard - 1) / nshard;
     const u64 a = lo + shard * span, b = std::min(hi, a + span);
@@ -297,6 +397,12 @@ int main(int argc, char **argv) {
     }
     fprintf(stderr, "[rung_scan3_gb300] autotune: short_max=%u rung_blocks_per_sm=%u\n", sc.short_max,
             sc.rung_blocks_per_sm);
+  }
+  if (meta) {
+    const int rc = write_meta(e, meta, lo, hi, M, seg, chunk_rounds, round_order, emit_surv, shard, nshard, ffile,
+                              threads, t0);
+    es_close(e);
+    return rc;
   }
   const auto t1 = std::chrono::steady_clock::now();
   std::vector<es_counters> cnt(wins.size());

@@ -217,6 +217,11 @@ es_status es_solve_direct_batch(es_engine *engine, const uint64_t *p, size_t cou
 es_status es_factor_batch(es_engine *engine, const uint64_t *n, size_t count, uint64_t *pr,
                           uint8_t *ex, uint8_t *k);
 
+/* SHA-256 of a host buffer as 64 lowercase hex digits and a terminating NUL in out (cap >= 65);
+ * returns 64, or 0 on a bad argument. Host only, no device needed: the digest a shard meta
+ * records for its certificate stream (tools/run19.sh:70-77, `sha256sum`). */
+size_t es_sha256_hex(const void *data, size_t n, char *out, size_t cap);
+
 /* Primality of count values already on the device, for callers that cannot allocate
  * device memory (a process whose device memory is all reserved up front, code where an
  * allocation may not block or fail at run time, a framework that owns every allocation).

@@ -61,6 +61,8 @@ def main():
     for f in ("w19_certificates.txt", "w64_summary.txt", "w64_head.txt", "w64_tail.txt"):
         shutil.copyfile(os.path.join(REF, "data", "rederive", "windows", f), os.path.join(HERE, "windows", f))
     shutil.copyfile(os.path.join(REF, "data", "sieve15", "SUMMARY.txt"), os.path.join(HERE, "sieve15_SUMMARY.txt"))
+    os.makedirs(os.path.join(HERE, "metas"), exist_ok=True)
+    shutil.copyfile(os.path.join(REF, "data", "c19", "shard_0.meta"), os.path.join(HERE, "metas", "c19_shard_0.meta"))
     with open(os.path.join(HERE, "class_tables.sha256"), "w") as f:
         for M in (120120, 2042040):
             f.write("%s  class_table_%d.txt\n" % (sha256(os.path.join(REF, "tables", "class_table_%d.txt" % M)), M))
@@ -115,9 +117,11 @@ def main():
         for name, binary, args in rows:
             rel = [os.path.relpath(a, HERE) if a.startswith(HERE) else a for a in args]
             f.write("gen/%s %s %s %s\n" % (name, sha256(os.path.join(gen, name)), binary, " ".join(rel)))
-        for d in ("filters", "decades", "windows"):
+        for d in ("filters", "decades", "windows", "metas"):
             for name in sorted(os.listdir(os.path.join(HERE, d))):
                 f.write("%s/%s %s copied\n" % (d, name, sha256(os.path.join(HERE, d, name))))
+        for name in ("sieve15_SUMMARY.txt",):
+            f.write("%s %s copied\n" % (name, sha256(os.path.join(HERE, name))))
     print("fixtures written to", HERE)
 
 
