@@ -352,6 +352,7 @@ def run_gpu(args, ws, rank, local):
     dev_ms, wall_s, launches, recs_n, items = 0.0, 0.0, 0, 0, 0
     stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
     kern = {"prep_ms": 0.0, "mark_short_ms": 0.0, "mark_long_ms": 0.0}
+    host = {"host_setup_ms": 0.0, "host_device_ms": 0.0, "host_collect_ms": 0.0}
     warr, carr = eng.make_windows(wins), eng.make_counters(len(wins))
     with Clocks(local) as clk:
         for _ in range(args.steps):
@@ -369,6 +370,8 @@ def run_gpu(args, ws, rank, local):
                 stage[k] += t[k]
             for k in kern:
                 kern[k] += t[k]
+            for k in host:
+                host[k] += t[k]
     barrier(ws)
     clocks = clk.summary()
     dev_s = allmax(ws, dev_ms / 1000.0)
@@ -433,7 +436,9 @@ def run_gpu(args, ws, rank, local):
                 "gpu_launches": launches, "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
                 "stages_ms_per_step": dict({k: v / args.steps for k, v in stage.items()},
                                            **{k: v / args.steps for k, v in kern.items()}),
-                "tail": {"survivors": int(last_t["survivors"]), "primes": int(last_t["primes"])}}
+                "tail": {"survivors": int(last_t["survivors"]), "primes": int(last_t["primes"])},
+                # where the e2e call's wall time goes (es_timing host fields), per step
+                "e2e_host_ms_per_step": {k[5:]: v / args.steps for k, v in host.items()}}
         line.update(extra)
         print(json.dumps(line))
     eng.close()

@@ -856,6 +856,10 @@ struct es_engine {
   es::u64 M = 0, mmax = 0, sieve_p = 0;
   uint32_t flags = 0;
   std::vector<es::u64> classes;
+  // host arithmetic on window bounds: classes below residue x are lane_at[x >> LANE_BLOCK_BITS]
+  // plus the few classes of x's block that lie below x; inv_M estimates division by M
+  std::vector<uint32_t> lane_at;
+  double inv_M = 0;
   es::u64 wheel_pmin = 0, cover_pmax = 0, class_fnv = 0, filter_fnv = 0;
   const es::ClassPin *pin = nullptr;
   std::vector<es::u64> mods, ress;     // certified filters [0,ncov) then stage-B' primes
@@ -990,6 +994,36 @@ static size_t mark_smem(const es_engine *e) {
   return ((4 * e->D + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
 }
 
+constexpr int LANE_BLOCK_BITS = 9;
+
+// Number of classes below x, 0 <= x <= M (lower_bound over the sorted classes, by table).
+static u64 classes_below(const es_engine *e, u64 x) {
+  u64 i = e->lane_at[x >> LANE_BLOCK_BITS];
+  while (i < e->classes.size() && e->classes[i] < x) ++i;
+  return i;
+}
+
+// x / M and x mod M for any 64-bit x: a double estimate of the quotient (off by at most
+// one: x / M < 2^44, and the product's relative error is 2^-52) corrected exactly.
+static void divmod_M(const es_engine *e, u64 x, u64 &q, u64 &r) {
+  const u64 M = e->M;
+  q = (u64)((double)x * e->inv_M);
+  const unsigned __int128 qm = (unsigned __int128)q * M;
+  if (qm > x) { --q; r = x - (u64)(qm - M); }
+  else { r = x - (u64)qm; if (r >= M) { ++q; r -= M; } }
+}
+
+static void build_lane_index(es_engine *e) {
+  const u64 nb = (e->M >> LANE_BLOCK_BITS) + 2;
+  e->lane_at.assign(nb, 0);
+  size_t i = 0;
+  for (u64 b = 0; b < nb; ++b) {
+    while (i < e->classes.size() && e->classes[i] < (b << LANE_BLOCK_BITS)) ++i;
+    e->lane_at[b] = (uint32_t)i;
+  }
+  e->inv_M = 1.0 / (double)e->M;
+}
+
 // Window descriptors and their marking items. Short windows (at most SEG_SMALL positions
 // per lane) go to k_mark_short, which walks them lane by lane; long windows get one lane per
 // item and segments of SEG_BIG positions in k_mark.
@@ -1002,8 +1036,10 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
   for (size_t i = 0; i < n; ++i) {
     WinDev &d = out[i];
     d.lo = w[i].lo; d.hi = std::max(w[i].lo, w[i].hi);
-    d.Q = d.lo / M;
-    d.lomod = (u32)(d.lo % M);
+    u64 q, r;
+    divmod_M(e, d.lo, q, r);
+    d.Q = q;
+    d.lomod = (u32)r;
     const u64 len = d.hi - d.lo;
     const u64 maxpos = len ? (len - 1) / M + 1 : 0;     // most positions any lane can hold
     d.item0 = items;
@@ -1015,11 +1051,14 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
         // a contiguous lane range unless it wraps past M.
         u64 la = 0, lb = L;
         if (len < M && d.lomod + len <= M) {
-          la = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod) - e->classes.begin();
-          lb = std::lower_bound(e->classes.begin(), e->classes.end(), (u64)d.lomod + len) - e->classes.begin();
+          la = classes_below(e, d.lomod);
+          lb = classes_below(e, d.lomod + len);
         }
-        if (la < lb)
-          shortw.push_back(ShortWin{d.Q, d.lomod, (u32)i, (u32)la, (u32)lb, (u32)(len / M), (u32)(len % M)});
+        if (la < lb) {
+          u64 lq, lr;
+          divmod_M(e, len, lq, lr);
+          shortw.push_back(ShortWin{d.Q, d.lomod, (u32)i, (u32)la, (u32)lb, (u32)lq, (u32)lr});
+        }
       }
     } else {
       d.seg = SEG_BIG; d.nseg = (u32)((maxpos + SEG_BIG - 1) / SEG_BIG); d.groups = (u32)L;
@@ -1033,10 +1072,13 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
 // of the remainder (the sum over lanes of sieve/rung_scan3.cpp:716's npos).
 static u64 positions_in(const es_engine *e, u64 lo, u64 hi) {
   if (hi <= lo) return 0;
-  const u64 M = e->M, len = hi - lo, a = lo % M, rem = len % M;
-  auto below = [&](u64 x) { return (u64)(std::lower_bound(e->classes.begin(), e->classes.end(), x) - e->classes.begin()); };
-  u64 part = a + rem <= M ? below(a + rem) - below(a) : (e->classes.size() - below(a)) + below(a + rem - M);
-  return (len / M) * e->classes.size() + part;
+  const u64 M = e->M;
+  u64 qa, a, ql, rem;
+  divmod_M(e, lo, qa, a);
+  divmod_M(e, hi - lo, ql, rem);
+  u64 part = a + rem <= M ? classes_below(e, a + rem) - classes_below(e, a)
+                          : (e->classes.size() - classes_below(e, a)) + classes_below(e, a + rem - M);
+  return ql * e->classes.size() + part;
 }
 
 // One pass of the funnel on the engine's stream: reset the counters, copy the batch header
@@ -1136,8 +1178,14 @@ static std::string status_text(u32 st) {
 
 // Runs windows through the funnel and collects counters and sorted records. Re-runs
 // with larger buffers when the survivor list overflowed (the count is exact even then).
+static double ms_since(std::chrono::steady_clock::time_point t) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+}
+
 static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
                              es_counters *per_window, es_records *recs) {
+  const auto t_start = std::chrono::steady_clock::now();
+  double setup_ms = 0, device_ms = 0;
   const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
   for (size_t i = 0; i < n; ++i) {
     if (w[i].hi > DIRECT_PMAX)
@@ -1148,8 +1196,9 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
   std::vector<WinDev> wd;
   std::vector<ShortWin> shortw;
   const u64 total_items = describe(e, w, n, wd, shortw);
+  std::vector<u64> npos(n);
   u64 positions_bound = 0;
-  for (size_t i = 0; i < n; ++i) positions_bound += positions_in(e, w[i].lo, w[i].hi);
+  for (size_t i = 0; i < n; ++i) positions_bound += (npos[i] = positions_in(e, w[i].lo, w[i].hi));
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
   cap = std::max(cap, sl->cap);
   const bool persistent = schedule == ES_SCHED_PERSISTENT;
@@ -1188,15 +1237,22 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
       if (!shortw.empty()) {
         // largest first: the warps of a k_mark_short CTA deal the windows round robin, so the
         // CTA's last window is a small one
-        std::vector<ShortWin> sorted(shortw);
-        auto work = [](const ShortWin &x) { return (u64)(x.lb - x.la) * (x.lq + 1); };
-        std::stable_sort(sorted.begin(), sorted.end(),
-                         [&](const ShortWin &x, const ShortWin &y) { return work(x) > work(y); });
-        memcpy(sl->h_short, sorted.data(), sorted.size() * sizeof(ShortWin));
+        // keys: descending work in the high bits, the original index (ties in order) below
+        std::vector<u64> key(shortw.size());
+        for (size_t k = 0; k < shortw.size(); ++k) {
+          const ShortWin &x = shortw[k];
+          const u64 work = (u64)(x.lb - x.la) * (x.lq + 1);          // < 2^21
+          key[k] = ((((u64)1 << 24) - 1 - work) << 32) | k;
+        }
+        std::sort(key.begin(), key.end());
+        for (size_t k = 0; k < key.size(); ++k) sl->h_short[k] = shortw[(u32)key[k]];
       }
       if (!sl->gexec) { s = capture_graph(e, sl); if (s) return s; }
+      setup_ms = ms_since(t_start);
+      const auto t_launch = std::chrono::steady_clock::now();
       CU(cudaGraphLaunch(sl->gexec, sl->stream));
       CU(cudaStreamSynchronize(sl->stream));
+      device_ms = ms_since(t_launch);
       launches = 7;
       s = collect();
       if (s) return s;
@@ -1246,7 +1302,7 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
   for (size_t i = 0; i < n; ++i) {      // the SUMMARY counters (sieve/rung_scan3.cpp:764-772)
     const WinCount &c = sl->h_cnt[i];
     es_counters &o = per_window[i];
-    o.positions = positions_in(e, w[i].lo, w[i].hi);
+    o.positions = npos[i];
     if (e->nf == e->ncov) { o.covered = o.positions - c.surv; o.sieved = 0; }
     else { o.covered = o.positions - c.after_covers; o.sieved = c.after_covers - c.surv; }
     o.mr = c.surv; o.composite = c.composite; o.rung = c.rung; o.direct = c.direct;
@@ -1264,6 +1320,9 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
     static_assert(sizeof(RecDev) == sizeof(es_record), "record layout");
     memcpy(recs->recs, hr.data(), hr.size() * sizeof(es_record));
   }
+  sl->timing.host_setup_ms = setup_ms;
+  sl->timing.host_device_ms = device_ms;
+  sl->timing.host_collect_ms = ms_since(t_start) - setup_ms - device_ms;
   return ES_OK;
 }
 
@@ -1617,6 +1676,7 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   const std::vector<Cover> covers = gen_covers(e->mmax);
   const Wheel w = build_wheel(e->M, gen_wheel_covers(e->M), gen_ucerts(UCERT_RMAX, UCERT_UMAX));
   e->classes = w.classes;
+  build_lane_index(e);
   e->wheel_pmin = w.max_pmin;
   for (const Cover &f : covers) e->cover_pmax = std::max(e->cover_pmax, f.pmin);
   e->class_fnv = fnv64_classes(e->classes);

@@ -80,7 +80,8 @@ class Timing(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("total_ms", "mark_ms", "mr_ms", "rung_ms", "direct_ms", "prep_ms",
                                           "mark_short_ms", "mark_long_ms")] + \
                [(n, C.c_uint64) for n in ("marks_kernel_launches", "kernel_launches", "mark_items", "survivors",
-                                          "primes", "short_pairs", "mask_bytes")]
+                                          "primes", "short_pairs", "mask_bytes")] + \
+               [(n, C.c_double) for n in ("host_setup_ms", "host_device_ms", "host_collect_ms")]
 
 
 _lib = None

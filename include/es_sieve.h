@@ -119,6 +119,9 @@ typedef struct {
   uint64_t mark_items, survivors, primes;
   uint64_t short_pairs;     /* (lane, short window) pairs, active or not, walked by k_mark_short */
   uint64_t mask_bytes;      /* kill-mask table bytes one k_mark_short launch reads */
+  /* host wall time of the call: describing and staging the windows, from the launch to the
+   * end of the device work (copies included), and collecting counters and records */
+  double host_setup_ms, host_device_ms, host_collect_ms;
 } es_timing_t;
 
 /* Batch schedules: per-window launches of the same kernels, or one persistent launch over
