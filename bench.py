@@ -39,9 +39,11 @@ import workloads  # noqa: E402
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
 METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
-# DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch, from the
-# ncu capture summarised in profiles/k_mark_short_batch4096_dram.md
-MARK_SHORT_TRAFFIC = None
+# DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch: one ncu
+# capture of this kernel on this workload (dram__bytes_read.sum 89.27 MB +
+# dram__bytes_write.sum 3.50 MB); scaled by the mask bytes when another batch size is run.
+MARK_SHORT_TRAFFIC_4096 = 89.270528e6 + 3.503872e6
+MARK_SHORT_INST_4096 = 1111276544            # smsp__inst_executed.sum of the same capture
 
 
 def parse():
@@ -407,7 +409,7 @@ def run_gpu(args, ws, rank, local):
     if dom == "k_mark_short":
         # one kill-mask row per lane from HBM, plus the per-window stride residues and window list
         alg = last_t["mask_bytes"] + len(wins) * 263 * 2 + len(wins) * 32
-        traffic = MARK_SHORT_TRAFFIC
+        traffic = MARK_SHORT_TRAFFIC_4096 * alg / 88992512 if args.windows != 4096 else MARK_SHORT_TRAFFIC_4096
     else:
         # the survivor tail: 24 B in and 64 B out per prime
         alg = int(last_t["primes"]) * (24 + 64)
@@ -415,7 +417,16 @@ def run_gpu(args, ws, rank, local):
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes": alg, "ms_per_launch": per_launch_ms,
-            "note": "issue-bound integer work: the HBM fraction is small by construction; see profiles/"}
+            "note": "issue-bound integer work: the HBM fraction is small by construction"}
+    if dom == "k_mark_short" and args.windows == 4096:
+        # The bound that binds: instruction issue. Warp instructions of one launch (ncu
+        # smsp__inst_executed.sum on this workload) over the live launch time, against 152 SMs x 4
+        # schedulers x one instruction per cycle at the sampled SM clock.
+        inst = MARK_SHORT_INST_4096
+        mhz = clocks.get("sm_mhz") or 2070.0
+        peak_issue = 152 * 4 * mhz * 1e6
+        roof["issue"] = {"achieved": inst / (per_launch_ms / 1000.0), "peak": peak_issue, "unit": "warp inst/s",
+                         "frac": inst / (per_launch_ms / 1000.0) / peak_issue, "inst_per_launch": inst}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
