@@ -30,6 +30,7 @@ enum : u32 {
   ST_STACK_OVERFLOW = 1u << 4,  // composite stack of the hard factorization overflowed
   ST_QUEUE_TIMEOUT = 1u << 5,   // a work-queue wait gave up
   ST_BAD_INPUT = 1u << 6,       // an argument outside the documented domain reached a kernel
+  ST_CERT_BAD = 1u << 7,        // a certificate failed its exact re-derivation (es_check.cuh)
 };
 
 constexpr int MAXF = 16;                       // census/rung_scan.cpp:147

@@ -21,6 +21,7 @@
 // reference's lane-major order per window.
 #include "../../include/es_sieve.h"
 #include "es_arith.cuh"
+#include "es_check.cuh"
 #include "es_kernels.cuh"
 #include "es_tail.cuh"
 #include "es_wheel.h"
@@ -695,7 +696,9 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
     const bool ok = !no_rung &&
                     block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B);
     if (threadIdx.x == 0) {
-      if (ok) {
+      if (ok && !check_rung_cert(s.p, res.A, res.r, res.u)) {
+        atomicOr(T.status, ST_CERT_BAD);            // never emitted
+      } else if (ok) {
         RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, res.A, res.r, res.u.lo, res.u.hi};
         put_record(T, rec);
         atomicAdd(&T.cnt[s.win].rung, 1ull);
@@ -717,6 +720,7 @@ __global__ void k_direct(const TailParams T) {
     const Surv s = T.surv[T.direct[i]];
     u64 a, c, d, k;
     if (solve_direct(s.p, a, c, d, k, T.tdp, T.tde, T.status)) {
+      if (!check_solved_cert(s.p, a, c, d, k)) { atomicOr(T.status, ST_CERT_BAD); continue; }
       RecDev rec{ES_REC_SOLVED, s.win, s.lane, 0, s.J, s.p, a, c, d, k};
       put_record(T, rec);
       atomicAdd(&T.cnt[s.win].direct, 1ull);
@@ -729,6 +733,18 @@ __global__ void k_direct(const TailParams T) {
 }
 
 // ---------------------------------------------------------------- probe kernels
+// Exact re-check of caller records (es_check_records): ok[i] = 1 for a RUNG or SOLVED
+// record whose identity holds, 0 otherwise (SURVIVOR and unknown kinds included).
+__global__ void k_probe_check(const RecDev *r, u64 count, unsigned char *ok) {
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
+    const RecDev x = r[i];
+    bool good = false;
+    if (x.kind == ES_REC_RUNG) good = check_rung_cert(x.p, x.a, x.b, U128{x.c, x.d});
+    else if (x.kind == ES_REC_SOLVED) good = check_solved_cert(x.p, x.a, x.b, x.c, x.d);
+    ok[i] = good;
+  }
+}
+
 __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
   const u32 lane = threadIdx.x & 31;
   const u64 warps = (u64)gridDim.x * blockDim.x / 32;
@@ -747,8 +763,9 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_probe_rung(const u64 *p,
   __shared__ RungResult slot[RUNG_WARPS];
   __shared__ RungResult res;
   for (u64 i = blockIdx.x; i < count; i += gridDim.x) {
-    const bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res);
+    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res);
     if (threadIdx.x == 0) {
+      if (ok && !check_rung_cert(p[i], res.A, res.r, res.u)) { atomicOr(status, ST_CERT_BAD); ok = false; }
       found[i] = ok;
       out[i] = ok ? RecDev{ES_REC_RUNG, 0, 0, 0, 0, p[i], res.A, res.r, res.u.lo, res.u.hi}
                   : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
@@ -760,7 +777,8 @@ __global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned ch
                                const u32 *tdp, const TdEntry *tde, u32 *status) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (u64)gridDim.x * blockDim.x) {
     u64 a, c, d, k;
-    const bool ok = solve_direct(p[i], a, c, d, k, tdp, tde, status);
+    bool ok = solve_direct(p[i], a, c, d, k, tdp, tde, status);
+    if (ok && !check_solved_cert(p[i], a, c, d, k)) { atomicOr(status, ST_CERT_BAD); ok = false; }
     found[i] = ok;
     out[i] = ok ? RecDev{ES_REC_SOLVED, 0, 0, 0, 0, p[i], a, c, d, k} : RecDev{0, 0, 0, 0, 0, p[i], 0, 0, 0, 0};
   }
@@ -1173,6 +1191,7 @@ static std::string status_text(u32 st) {
   if (st & ST_STACK_OVERFLOW) s += " factor-stack";
   if (st & ST_QUEUE_TIMEOUT) s += " queue-timeout";
   if (st & ST_BAD_INPUT) s += " bad-input";
+  if (st & ST_CERT_BAD) s += " certificate-self-check";
   return s;
 }
 
@@ -1967,6 +1986,16 @@ es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_
                  k_probe_factor<<<e->sm_count * 4, 128, 0, e->slots[0].stream>>>((const u64 *)in, count, (u64 *)o[0],
                                                                        (unsigned char *)o[1], (unsigned char *)o[2],
                                                                        e->d_tdp, e->d_tde, e->slots[0].d_status);
+               });
+}
+
+es_status es_check_records(es_engine *e, const es_record *r, size_t count, uint8_t *ok) {
+  if (!e || (!r && count) || (!ok && count)) return ES_ERR_ARG;
+  if (!count) return ES_OK;
+  return probe(e, &e->slots[0], count, count * sizeof(es_record), r, 0, {{ok, count}},
+               [&](void *in, std::vector<void *> &o) {
+                 k_probe_check<<<e->sm_count * 4, 256, 0, e->slots[0].stream>>>((const RecDev *)in, count,
+                                                                              (unsigned char *)o[0]);
                });
 }
 

@@ -121,6 +121,8 @@ def load_library(path=LIB_PATH):
         "es_solve_rung_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(Record), P(C.c_uint8)]),
         "es_solve_direct_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(Record), P(C.c_uint8)]),
         "es_factor_batch": (C.c_int, [e, P(C.c_uint64), C.c_size_t, P(C.c_uint64), P(C.c_uint8), P(C.c_uint8)]),
+        "es_check_records": (C.c_int, [e, P(Record), C.c_size_t, P(C.c_uint8)]),
+        "es_sha256_hex": (C.c_size_t, [C.c_void_p, C.c_size_t, C.c_char_p, C.c_size_t]),
         "es_is_prime_noalloc": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
@@ -339,6 +341,14 @@ class Engine:
     def solve_direct(self, ps):
         """Certificate line per prime (solve_direct3), or None."""
         return self._solve(self.lib.es_solve_direct_batch, ps)
+
+    def check_records(self, recs):
+        """Device re-check of certificate records (a RECORD_DTYPE array): a bool array."""
+        a = np.ascontiguousarray(recs, dtype=RECORD_DTYPE)
+        out = np.zeros(len(a), dtype=np.uint8)
+        self._check(self.lib.es_check_records(self.h, a.ctypes.data_as(C.POINTER(Record)), len(a),
+                                              out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out.astype(bool)
 
     def factor(self, ns):
         a = np.ascontiguousarray(ns, dtype=np.uint64)

@@ -219,6 +219,12 @@ es_status es_solve_direct_batch(es_engine *engine, const uint64_t *p, size_t cou
                                 uint8_t *found);
 es_status es_factor_batch(es_engine *engine, const uint64_t *n, size_t count, uint64_t *pr,
                           uint8_t *ex, uint8_t *k);
+/* Exact re-check of certificates on the device (the identity sieve/verify_covers.py:246-275
+ * tests with rationals, in fixed-width integers): ok[i] = 1 when record i is a RUNG or SOLVED
+ * certificate whose decomposition of 4/p holds, 0 otherwise (SURVIVOR records included). The
+ * engine runs the same check on every certificate before emitting it; a failure there is
+ * ES_ERR_DEVICE_STATUS ("certificate-self-check") and the certificate is not emitted. */
+es_status es_check_records(es_engine *engine, const es_record *recs, size_t count, uint8_t *ok);
 
 /* SHA-256 of a host buffer as 64 lowercase hex digits and a terminating NUL in out (cap >= 65);
  * returns 64, or 0 on a bad argument. Host only, no device needed: the digest a shard meta

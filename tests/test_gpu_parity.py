@@ -263,3 +263,44 @@ def test_every_emitted_certificate_rechecks_in_exact_arithmetic():
         assert bad == 0 and surv == 0
         total += r + s_
     assert total > 9000
+
+
+def _records_from_text(text):
+    recs = []
+    for ln in text.splitlines():
+        t = ln.split()
+        if not t or t[0] == "SUMMARY":
+            continue
+        if t[0] == "RUNG":
+            p, A, r, u = map(int, t[1:5])
+            recs.append((es_sieve.ES_REC_RUNG, 0, 0, 0, 0, p, A, r, u & (2 ** 64 - 1), u >> 64))
+        elif t[0] == "SOLVED":
+            p, a, c, d, k = map(int, t[1:6])
+            recs.append((es_sieve.ES_REC_SOLVED, 0, 0, 0, 0, p, a, c, d, k))
+        elif t[0] == "SURVIVOR":
+            recs.append((es_sieve.ES_REC_SURVIVOR, 0, 0, 0, 0, int(t[1]), 0, 0, 0, 0))
+    return np.array(recs, dtype=es_sieve.RECORD_DTYPE)
+
+
+def test_device_certificate_check_on_reference_records_and_planted_mistakes():
+    """es_check_records re-derives each identity on the device: every certificate the
+    reference emitted (w19, c3, cover_scan's stage-E rows) passes; copies with one field
+    changed (planted here, on the CPU) and SURVIVOR lines fail."""
+    good = np.concatenate([_records_from_text(read("windows", "w19_certificates.txt")),
+                           _records_from_text(read("gen", "c3_gpu.out")),
+                           _records_from_text(read("gen", "d3_120120_m200_norung_cover_scan.out"))])
+    assert (good["kind"] == es_sieve.ES_REC_SOLVED).sum() > 0 and len(good) > 8500
+    assert engine().check_records(good).all()
+    bad = []
+    for field in ("a", "b", "c", "d"):
+        x = good[:64].copy()
+        x[field] += 1
+        bad.append(x)
+    x = good[:8].copy()
+    x["p"] += 2
+    bad.append(x)
+    bad = np.concatenate(bad)
+    assert not engine().check_records(bad).any()
+    s = good[:4].copy()
+    s["kind"] = es_sieve.ES_REC_SURVIVOR
+    assert not engine().check_records(s).any()
