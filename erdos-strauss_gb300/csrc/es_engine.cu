@@ -328,66 +328,69 @@ __device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFF
 // by r mod 32. After each round the warp ORs its kill words into alive, and it stops as soon
 // as nothing is left alive: the strides come densest first, so most segments are dead after
 // one or two rounds. Returns nonzero if a position is still alive.
-__device__ __forceinline__ MaskDesc mask_desc(const MaskDesc *smd, const MaskDesc *__restrict__ mdesc, u32 k) {
-  if (smd) return smd[k];
-  const uint4 mv = __ldg(reinterpret_cast<const uint4 *>(mdesc) + k);
-  return MaskDesc{mv.x, mv.y, mv.z, mv.w};
-}
 
 template <int NC>
 __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], const u32 (&b)[SHORT_LANES],
-                                                 const u32 *tab, u32 tab_words, const MaskDesc *smd,
-                                                 const MaskDesc *__restrict__ mdesc, u32 m0, u32 m1,
-                                                 const u16 *__restrict__ Qrow, u32 q0_first, u32 lane) {
-  u32 any = 0;
-  #pragma unroll
-  for (int q = 0; q < SHORT_LANES; ++q)
-    #pragma unroll
-    for (int c = 0; c < NC; ++c) any |= alive[q][c];
+                                                 const u32 *tab, u32 tab_words, const MaskDesc *smd, u32 m0,
+                                                 u32 m1, const u16 *__restrict__ Qrow, u32 q0_first, u32 lane) {
   u32 kill[SHORT_LANES][NC];
-  // ORs stride k's kill bits into kill: every chunk with one load each in the first round,
-  // only the chunks still alive afterwards
-  auto extract = [&](u32 k, u32 q0, bool first) {
-    const MaskDesc md = mask_desc(smd, mdesc, k);
-    const u32 s = md.s;
+  // Round one (strides m0 .. m0 + 31, q0_first loaded by the caller ahead of time): every
+  // chunk, one mask word load per chunk, no per-chunk tests.
+  u32 k = m0 + lane;
+  u32 q0 = k + 32 < m1 ? (u32)__ldg(Qrow + smd[k + 32].d) : 0u;    // the next round's residue
+  if (k < m1) {
+    const MaskDesc md = smd[k];
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q) {
-      u32 r = q0 + b[q];
-      r = r >= s ? r - s : r;
+      u32 r = q0_first + b[q];
+      r = r >= md.s ? r - md.s : r;
       // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
       const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
       const u32 sh = r & 31;
-      if (first) {
-        u32 w0 = wp[0];
-        #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-          const u32 w1 = wp[c + 1];
-          kill[q][c] |= __funnelshift_r(w0, w1, sh);
-          w0 = w1;
-        }
-      } else {
-        #pragma unroll
-        for (int c = 0; c < NC; ++c)
-          if (alive[q][c]) kill[q][c] |= __funnelshift_r(wp[c], wp[c + 1], sh);
+      u32 w0 = wp[0];
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const u32 w1 = wp[c + 1];
+        kill[q][c] = __funnelshift_r(w0, w1, sh);
+        w0 = w1;
       }
     }
-  };
-  // q0_first: this lane's segment-start residue for stride m0 + lane, loaded by the caller
-  // ahead of time; each round loads the next round's while it works
-  u32 q0 = q0_first;
-  bool first = true;
-  for (u32 kb = m0; kb < m1 && any;) {
+  } else {
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q)
       #pragma unroll
       for (int c = 0; c < NC; ++c) kill[q][c] = 0;
-    const u32 k = kb + lane;
-    u32 q0_next = 0;
-    if (k + 32 < m1) q0_next = (u32)__ldg(Qrow + mask_desc(smd, mdesc, k + 32).d);
-    if (k < m1) extract(k, q0, first);
+  }
+  u32 any = 0;
+  #pragma unroll
+  for (int q = 0; q < SHORT_LANES; ++q)
+    #pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      alive[q][c] &= ~warp_or32(kill[q][c]);
+      any |= alive[q][c];
+    }
+  // Later rounds, rarely more than one or two: only the chunks still alive.
+  for (u32 kb = m0 + 32; kb < m1 && any; kb += 32) {
+    k = kb + lane;
+    const u32 q0_next = k + 32 < m1 ? (u32)__ldg(Qrow + smd[k + 32].d) : 0u;
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) kill[q][c] = 0;
+    if (k < m1) {
+      const MaskDesc md = smd[k];
+      #pragma unroll
+      for (int q = 0; q < SHORT_LANES; ++q) {
+        u32 r = q0 + b[q];
+        r = r >= md.s ? r - md.s : r;
+        const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+        const u32 sh = r & 31;
+        #pragma unroll
+        for (int c = 0; c < NC; ++c)
+          if (alive[q][c]) kill[q][c] = __funnelshift_r(wp[c], wp[c + 1], sh);
+      }
+    }
     q0 = q0_next;
-    kb += 32;
-    first = false;
     any = 0;
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q)
@@ -440,7 +443,7 @@ __device__ __forceinline__ u32 short_phase(u32 (&alive)[SHORT_LANES][NC], const 
                                            const u32 (&n)[SHORT_LANES], const u32 (&b)[SHORT_LANES],
                                            const u16 *const (&K0row)[SHORT_LANES], const u16 *Qrow, u32 q0_first,
                                            u32 lane) {
-  const u32 any = short_mask_rounds<NC>(alive, b, tab, tab_words, smd, P.mdesc, m0, m1, Qrow, q0_first, lane);
+  const u32 any = short_mask_rounds<NC>(alive, b, tab, tab_words, smd, m0, m1, Qrow, q0_first, lane);
   if (any && l1 > l0) {
     u32 kill[SHORT_LANES][NC];
     #pragma unroll
@@ -491,7 +494,7 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
   if (cnt && (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov)) {          // stage B'
     if (lane == 0) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
     const u32 k = P.nm_cov + lane;
-    const u32 q0b = k < P.nm_all ? (u32)__ldg(Qrow + mask_desc(smd, P.mdesc, k).d) : 0u;
+    const u32 q0b = k < P.nm_all ? (u32)__ldg(Qrow + smd[k].d) : 0u;
     cnt = short_phase<NC>(alive, P, tab, tab_words, smd, P.nm_cov, P.nm_all, P.nl_cov, P.nl_all, n, b, K0row, Qrow,
                           q0b, lane);
   }
@@ -531,11 +534,9 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
   const u32 lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (P.hdr->nshort == 0) return;
   const u32 tab_words = P.Wpad * 2;                    // 32-bit words per lane table
-  MaskDesc *smd = nullptr;
-  if (P.nm_all <= SMD_MAX) {
-    smd = reinterpret_cast<MaskDesc *>(tab + SHORT_LANES * tab_words);
-    for (u32 k = threadIdx.x; k < P.nm_all; k += BLOCK) smd[k] = P.mdesc[k];
-  }
+  // the stride descriptors (at most SMD_MAX, the host keeps any further strides unmasked)
+  MaskDesc *smd = reinterpret_cast<MaskDesc *>(tab + SHORT_LANES * tab_words);
+  for (u32 k = threadIdx.x; k < P.nm_all; k += BLOCK) smd[k] = P.mdesc[k];
   const u32 nshort = P.hdr->nshort;
   for (u32 l0 = blockIdx.x * SHORT_LANES; l0 < P.L; l0 += gridDim.x * SHORT_LANES) {
     for (int q = 0; q < SHORT_LANES; ++q) {
@@ -560,7 +561,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
     // round's stride residue of the next window is loaded while a window is marked.
     constexpr u32 WS = BLOCK / 32;
     const uint4 *sw4 = reinterpret_cast<const uint4 *>(P.shortw);
-    const u32 d_first = lane < P.nm_cov ? mask_desc(smd, P.mdesc, lane).d : 0u;
+    const u32 d_first = lane < P.nm_cov ? smd[lane].d : 0u;
     auto load_q0 = [&](u32 wi) {
       return lane < P.nm_cov ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + d_first) : 0u;
     };
@@ -1005,7 +1006,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
 }
 
 static size_t short_smem(const es_engine *e) {
-  return (size_t)SHORT_LANES * e->Wpad * 8 + (e->nm_all <= SMD_MAX ? e->nm_all * sizeof(MaskDesc) : 0);
+  return (size_t)SHORT_LANES * e->Wpad * 8 + (size_t)e->nm_all * sizeof(MaskDesc);
 }
 
 static size_t mark_smem(const es_engine *e) {
@@ -1471,7 +1472,7 @@ static es_status build_tables(es_engine *e) {
         // bits [0, s + SEG_SMALL) plus one spare word: a segment of up to SEG_SMALL positions
         // starting at any residue below s reads words r/32 .. r/32 + SEG_SMALL/32 of the slice
         const u32 wd = (st + SEG_SMALL + 31) / 32 + 1;
-        if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX) break;
+        if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX || md.size() >= SMD_MAX) break;
         const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
         md.push_back(MaskDesc{st, di, words, 32 % st});
         words += wd;
