@@ -671,6 +671,12 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
 }
 
 constexpr int RUNG_WARPS = 4;
+#ifndef ES_HELP_BLOCKS_PER_SM
+#define ES_HELP_BLOCKS_PER_SM 1
+#endif
+#ifndef ES_HELP_BLOCKS_DIV
+#define ES_HELP_BLOCKS_DIV 1
+#endif
 
 // Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung). Blocks take primes
 // from a queue; a block that finds it empty turns its warps into helpers on the hard board
@@ -712,7 +718,11 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
     }
     __syncthreads();
   }
-  if (!no_rung) warp_help(B, threadIdx.x & 31);
+  // Helpers come from the first help_blocks blocks only (one per SM): the walks of a hard
+  // cofactor progress at the issue rate their sub-partition gives them, so helpers beyond
+  // one warp per scheduler would only split that rate over more walks, and the expected wait
+  // for the first collision grows with the square root of the number of walks sharing it.
+  if (!no_rung && blockIdx.x < T.help_blocks) warp_help(B, threadIdx.x & 31);
 }
 
 __global__ void k_direct(const TailParams T) {
@@ -1000,6 +1010,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.recs = sl->d_recs; T.rec_count = sl->d_ctr + 4;
   T.rung_next = sl->d_ctr + 6; T.rung_done = sl->d_ctr + 7; T.help_sessions = sl->d_ctr + 8;
   T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
+  T.help_blocks = (u32)(e->sm_count * ES_HELP_BLOCKS_PER_SM / ES_HELP_BLOCKS_DIV);
   T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;
   T.cap = sl->cap;
   return T;

@@ -133,6 +133,7 @@ struct TailParams {
   unsigned long long *rung_done;      // primes k_rung has finished
   unsigned long long *help_sessions;  // helping sessions started on the hard board
   struct HardSlot *board;             // [HARD_SLOTS] cofactors whose rho takes long
+  u32 help_blocks;                    // k_rung blocks [0, help_blocks) help on the board
 };
 
 }  // namespace es
