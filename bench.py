@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--windows", type=int, default=4096)
+    ap.add_argument("--sieve", type=int, default=0, help="stage B' small primes up to P (rung_scan3 --sieve P)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -344,7 +345,7 @@ def run_gpu(args, ws, rank, local):
     import es_sieve
     flush, flush_note = l2_flusher(local)
     mods, ress = es_sieve.load_filters(GPU_TABLE)
-    eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local)
+    eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local, sieve_p=args.sieve)
     wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
     n_int = integers(wins)
     schedule = eng.autotune(wins, repeats=2) if not args.no_autotune else eng.schedule()
@@ -438,6 +439,7 @@ def run_gpu(args, ws, rank, local):
                 "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
                 "config": {"workload": "batch4096", "windows": args.windows, "integers_per_step": n_int,
                            "wheel": 2042040, "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED,
+                           "sieve": args.sieve,
                            "schedule": "persistent", "kernel_schedule": schedule, "l2": flush_note,
                            "parallelism": "replicas x%d" % ws},
                 # copied every step: batch header, window and short-window descriptors in; run
