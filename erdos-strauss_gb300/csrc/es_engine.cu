@@ -896,7 +896,7 @@ struct es_engine {
   // marking order: filters sorted by stride within each phase
   std::vector<uint32_t> order;
   uint32_t nf = 0, ldk = 0, D = 0, Dq = 0, Lpad = 0;
-  es_schedule sched{es::SEG_SMALL, 6, {0, 0, 0, 0, 0, 0}};   // es_set_schedule / es_autotune
+  es_schedule sched{es::SEG_SMALL, 6, 1, {0, 0, 0, 0, 0}};   // es_set_schedule / es_autotune
   int device = 0, sm_count = 0, mark_occupancy = 0;
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
@@ -1213,8 +1213,8 @@ static double ms_since(std::chrono::steady_clock::time_point t) {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
 }
 
-static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
-                             es_counters *per_window, es_records *recs) {
+static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
+                                    es_counters *per_window, es_records *recs) {
   const auto t_start = std::chrono::steady_clock::now();
   double setup_ms = 0, device_ms = 0;
   const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
@@ -1354,6 +1354,99 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
   sl->timing.host_setup_ms = setup_ms;
   sl->timing.host_device_ms = device_ms;
   sl->timing.host_collect_ms = ms_since(t_start) - setup_ms - device_ms;
+  return ES_OK;
+}
+
+// Windows whose lanes hold more than short_max positions are, by default, cut into
+// sub-windows of short_max positions per lane (short_max * M integers; the last one
+// shorter), which the short-window kernel marks with its early exit; with long_split = 0
+// they keep one device window each and go to the segment marking. Sub-window t of a window
+// starts t * short_max positions into every lane, so its records map back to the window by
+// J += t * short_max, and its counters add up to the window's (every counter is a sum over
+// positions). Device windows are run in passes of at most PASS_WINDOWS.
+constexpr size_t PASS_WINDOWS = 1u << 18;
+
+static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
+                             es_counters *per_window, es_records *recs) {
+  const u64 M = e->M, S = e->sched.short_max;
+  const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
+  bool split = false;
+  for (size_t i = 0; i < n; ++i) {                 // refuse what a run would refuse, first
+    if (w[i].hi > DIRECT_PMAX)
+      return fail(e, ES_ERR_RANGE, "HI must not exceed the stage-E ceiling " + std::to_string(DIRECT_PMAX));
+    if (w[i].lo <= floor_)
+      return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
+    const u64 len = w[i].hi > w[i].lo ? w[i].hi - w[i].lo : 0;
+    if (e->sched.long_split && len && (len - 1) / M + 1 > S) split = true;
+  }
+  if (!split) return run_device_windows(e, sl, w, n, schedule, per_window, recs);
+  memset(per_window, 0, n * sizeof(es_counters));
+  std::vector<es_record> all;
+  es_timing_t tot{};
+  std::vector<es_window> dw;
+  std::vector<std::pair<u32, u64>> dmap;          // (window, position offset) per device window
+  dw.reserve(PASS_WINDOWS);
+  dmap.reserve(PASS_WINDOWS);
+  // device windows are produced a pass at a time: (i, t) is the next sub-window to emit
+  size_t i = 0;
+  u64 t = 0;
+  while (i < n) {
+    dw.clear();
+    dmap.clear();
+    while (i < n && dw.size() < PASS_WINDOWS) {
+      const u64 lo = w[i].lo, hi = std::max(w[i].lo, w[i].hi);
+      const u64 len = hi - lo, maxpos = len ? (len - 1) / M + 1 : 0;
+      if (!e->sched.long_split || maxpos <= S) {
+        dw.push_back({lo, hi});
+        dmap.push_back({(u32)i, 0});
+        ++i;
+        continue;
+      }
+      const u64 step = S * M, a = lo + t * step;  // t * step < len: no overflow
+      dw.push_back({a, a + std::min(step, hi - a)});
+      dmap.push_back({(u32)i, t * S});
+      if (hi - a <= step) { ++i; t = 0; } else ++t;
+    }
+    const size_t m = dw.size();
+    std::vector<es_counters> pc(m);
+    es_records pr{nullptr, 0};
+    const es_status st = run_device_windows(e, sl, dw.data(), m, schedule, pc.data(), recs ? &pr : nullptr);
+    if (st != ES_OK) { es_free_records(&pr); return st; }
+    for (size_t k = 0; k < m; ++k) {
+      es_counters &o = per_window[dmap[k].first];
+      const es_counters &c = pc[k];
+      o.positions += c.positions; o.covered += c.covered; o.sieved += c.sieved; o.mr += c.mr;
+      o.composite += c.composite; o.rung += c.rung; o.direct += c.direct; o.survivors += c.survivors;
+    }
+    for (size_t r = 0; r < pr.n; ++r) {
+      es_record x = pr.recs[r];
+      const auto &mp = dmap[x.window];
+      x.window = mp.first;
+      x.J += mp.second;
+      all.push_back(x);
+    }
+    es_free_records(&pr);
+    const es_timing_t &tt = sl->timing;
+    tot.total_ms += tt.total_ms; tot.mark_ms += tt.mark_ms; tot.mr_ms += tt.mr_ms; tot.rung_ms += tt.rung_ms;
+    tot.direct_ms += tt.direct_ms; tot.prep_ms += tt.prep_ms; tot.mark_short_ms += tt.mark_short_ms;
+    tot.mark_long_ms += tt.mark_long_ms; tot.marks_kernel_launches += tt.marks_kernel_launches;
+    tot.kernel_launches += tt.kernel_launches; tot.mark_items += tt.mark_items; tot.survivors += tt.survivors;
+    tot.primes += tt.primes; tot.short_pairs += tt.short_pairs; tot.mask_bytes += tt.mask_bytes;
+    tot.host_setup_ms += tt.host_setup_ms; tot.host_device_ms += tt.host_device_ms;
+    tot.host_collect_ms += tt.host_collect_ms;
+  }
+  sl->timing = tot;
+  if (recs) {
+    std::sort(all.begin(), all.end(), [](const es_record &x, const es_record &y) {
+      if (x.window != y.window) return x.window < y.window;
+      if (x.lane != y.lane) return x.lane < y.lane;
+      return x.J < y.J;
+    });
+    recs->n = all.size();
+    recs->recs = (es_record *)malloc(std::max<size_t>(all.size(), 1) * sizeof(es_record));
+    if (!recs->recs) return fail(e, ES_ERR_NOMEM, "host records");
+    memcpy(recs->recs, all.data(), all.size() * sizeof(es_record));
+  }
   return ES_OK;
 }
 
@@ -1879,6 +1972,7 @@ es_status es_set_schedule(es_engine *e, const es_schedule *s) {
   if (s->short_max < 1 || s->short_max > es::SEG_SMALL) return fail(e, ES_ERR_ARG, "short_max must be in 1..256");
   if (s->rung_blocks_per_sm < 1 || s->rung_blocks_per_sm > 16)
     return fail(e, ES_ERR_ARG, "rung_blocks_per_sm must be in 1..16");
+  if (s->long_split > 1) return fail(e, ES_ERR_ARG, "long_split must be 0 or 1");
   for (uint32_t r : s->reserved)
     if (r) return fail(e, ES_ERR_ARG, "reserved schedule fields must be zero");
   // every slot idle while the schedule changes; their graphs hold the old launch shapes
@@ -1894,6 +1988,7 @@ es_status es_autotune(es_engine *e, const es_window *w, size_t n, int repeats, e
   if (!e || !w || n == 0 || repeats < 1 || repeats > 1000) return ES_ERR_ARG;
   static const uint32_t SHORT[] = {64, 128, 256};
   static const uint32_t RUNG[] = {4, 6, 8};
+  static const uint32_t SPLIT[] = {1, 0};
   const es_schedule before = e->sched;
   std::vector<es_counters> base(n), cur(n);
   es_records rbase{nullptr, 0};
@@ -1902,10 +1997,12 @@ es_status es_autotune(es_engine *e, const es_window *w, size_t n, int repeats, e
   bool first = true;
   es_status st = ES_OK;
   for (uint32_t sm : SHORT) {
-    for (uint32_t rb : RUNG) {
+    for (size_t cand = 0; cand < 6; ++cand) {
+      const uint32_t rb = RUNG[cand % 3], split = SPLIT[cand / 3];
       es_schedule c = before;
       c.short_max = sm;
       c.rung_blocks_per_sm = rb;
+      c.long_split = split;
       if ((st = es_set_schedule(e, &c)) != ES_OK) break;
       double ms = 1e300;
       for (int r = 0; r <= repeats && st == ES_OK; ++r) {

@@ -70,10 +70,12 @@ class Info(C.Structure):
 
 
 class Schedule(C.Structure):
-    _fields_ = [("short_max", C.c_uint32), ("rung_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("short_max", C.c_uint32), ("rung_blocks_per_sm", C.c_uint32), ("long_split", C.c_uint32),
+                ("reserved", C.c_uint32 * 5)]
 
     def as_dict(self):
-        return {"short_max": int(self.short_max), "rung_blocks_per_sm": int(self.rung_blocks_per_sm)}
+        return {"short_max": int(self.short_max), "rung_blocks_per_sm": int(self.rung_blocks_per_sm),
+                "long_split": int(self.long_split)}
 
 
 class Timing(C.Structure):
@@ -269,13 +271,15 @@ class Engine:
         self._check(self.lib.es_get_schedule(self.h, C.byref(sc)))
         return sc.as_dict()
 
-    def set_schedule(self, short_max=None, rung_blocks_per_sm=None):
+    def set_schedule(self, short_max=None, rung_blocks_per_sm=None, long_split=None):
         sc = Schedule()
         self._check(self.lib.es_get_schedule(self.h, C.byref(sc)))
         if short_max is not None:
             sc.short_max = short_max
         if rung_blocks_per_sm is not None:
             sc.rung_blocks_per_sm = rung_blocks_per_sm
+        if long_split is not None:
+            sc.long_split = long_split
         self._check(self.lib.es_set_schedule(self.h, C.byref(sc)))
 
     def autotune(self, windows, repeats=2):

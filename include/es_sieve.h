@@ -184,14 +184,18 @@ typedef struct {
                                     are marked by the short-window kernel, longer ones by the
                                     segment marking; default 256 */
   uint32_t rung_blocks_per_sm;   /* stage-D grid in blocks per SM (1..16); default 6 */
-  uint32_t reserved[6];          /* zero */
+  uint32_t long_split;           /* 1 (default): longer windows are cut into sub-windows of
+                                    short_max positions per lane for the short-window kernel;
+                                    0: they go to the segment marking */
+  uint32_t reserved[5];          /* zero */
 } es_schedule;
 
 es_status es_get_schedule(const es_engine *engine, es_schedule *out);
 /* ES_ERR_ARG for a value out of range; captured batch graphs are rebuilt on the next run. */
 es_status es_set_schedule(es_engine *engine, const es_schedule *s);
 /* Autotuner: runs the windows (persistent schedule) under each candidate schedule -- short_max
- * in {64, 128, 256} x rung_blocks_per_sm in {4, 6, 8} -- once to warm up and `repeats` times
+ * in {64, 128, 256} x rung_blocks_per_sm in {4, 6, 8} x long_split in {1, 0} -- once to warm up
+ * and `repeats` times
  * timed, keeps the best device time of each, checks that every candidate gave identical
  * counters and records (ES_ERR_DEVICE_STATUS if not), and sets the fastest. `chosen` may be
  * null. */

@@ -34,16 +34,35 @@ def _windows():
 
 def test_every_schedule_gives_identical_results(eng):
     wins = _windows()
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6)
+    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=0)
     base_c, base_r = eng.run_batch(wins)
-    for sm in (1, 32, 64, 128, 200, 256):
-        for rb in (1, 4, 8, 16):
-            eng.set_schedule(short_max=sm, rung_blocks_per_sm=rb)
-            for sched in (es_sieve.ES_SCHED_PERSISTENT, es_sieve.ES_SCHED_PLAIN):
-                c, r = eng.run_batch(wins, schedule=sched)
-                assert c == base_c, (sm, rb, sched)
-                assert r.tobytes() == base_r.tobytes(), (sm, rb, sched)
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6)
+    for split in (0, 1):
+        for sm in (1, 32, 64, 128, 200, 256):
+            for rb in (1, 4, 8, 16):
+                eng.set_schedule(short_max=sm, rung_blocks_per_sm=rb, long_split=split)
+                for sched in (es_sieve.ES_SCHED_PERSISTENT, es_sieve.ES_SCHED_PLAIN):
+                    c, r = eng.run_batch(wins, schedule=sched)
+                    assert c == base_c, (split, sm, rb, sched)
+                    assert r.tobytes() == base_r.tobytes(), (split, sm, rb, sched)
+    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=1)
+
+
+def test_long_windows_split_or_segmented_agree(eng):
+    """Windows of 2^34 to 2^40 integers (8 K to 540 K positions per lane, so thousands of
+    sub-windows) under both long-window schedules, against each other and against the
+    golden c3 stream."""
+    wins = [(workloads.c3()["lo"], workloads.c3()["hi"]), (10 ** 16 + 7, 10 ** 16 + 7 + (1 << 40)),
+            (255255 + 1, 255255 + 1 + (1 << 38))]
+    out = {}
+    for split in (1, 0):
+        eng.set_schedule(long_split=split)
+        out[split] = eng.run_batch(wins)
+    eng.set_schedule(long_split=1)
+    assert out[0][0] == out[1][0]
+    assert out[0][1].tobytes() == out[1][1].tobytes()
+    c, r = out[1]
+    mine = r[r["window"] == 0]
+    assert eng.text(wins[0][0], wins[0][1], c[0], mine) == read("gen", "c3_gpu.out")
 
 
 def test_autotune_picks_a_candidate_and_keeps_results(eng):
@@ -51,6 +70,7 @@ def test_autotune_picks_a_candidate_and_keeps_results(eng):
     before_c, before_r = eng.run_batch(wins)
     chosen = eng.autotune(wins, repeats=1)
     assert chosen["short_max"] in (64, 128, 256) and chosen["rung_blocks_per_sm"] in (4, 6, 8)
+    assert chosen["long_split"] in (0, 1)
     assert eng.schedule() == chosen
     c, r = eng.run_batch(wins)
     assert c == before_c and r.tobytes() == before_r.tobytes()
@@ -62,7 +82,10 @@ def test_schedule_refusals(eng):
         with pytest.raises(es_sieve.EsError) as ex:
             eng.set_schedule(**kw)
         assert ex.value.status == es_sieve.ES_ERR_ARG
-    assert eng.schedule() == {"short_max": 256, "rung_blocks_per_sm": 6}
+    assert eng.schedule() == {"short_max": 256, "rung_blocks_per_sm": 6, "long_split": 1}
+    with pytest.raises(es_sieve.EsError) as ex:
+        eng.set_schedule(long_split=2)
+    assert ex.value.status == es_sieve.ES_ERR_ARG
     with pytest.raises(es_sieve.EsError) as ex:
         eng.autotune([], repeats=1)
     assert ex.value.status == es_sieve.ES_ERR_ARG
