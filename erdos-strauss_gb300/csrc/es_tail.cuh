@@ -333,6 +333,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
     }
     if (nx >= NTD) break;
     if (dn * dn > cur) { complete = false; break; }   // cur is 1 or prime
+    if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;   // moot rung
   }
   if (cur > 1) {
     if (!complete || cur <= 0xFFFFFFFFull) {
@@ -346,6 +347,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         if (guard > 16) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
         const u64 v = stack[--sp];
         if (v == 1) continue;
+        if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;
         if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
         const u64 s = isqrt64(v);
         if (s * s == v) { wf_add(F, s, 2, lane); continue; }
