@@ -56,9 +56,10 @@ def build(verbose=False, ptxas_info=False):
         futs = [ex.submit(_run, cmd + [os.path.join(BUILD, o)]) for o, cmd in objs.items()]
         for f in futs:
             logs.append(f.result())
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB, os.path.join(BUILD, "es_engine.o"), os.path.join(BUILD, "es_noalloc.o"),
+    _run([nvcc] + ARCH + ["-shared", "-ldl", "-o", LIB, os.path.join(BUILD, "es_engine.o"), os.path.join(BUILD, "es_noalloc.o"),
                           os.path.join(BUILD, "es_wheel.o"), os.path.join(BUILD, "es_digest.o")])
-    _run(["g++", "-o", CLI, os.path.join(BUILD, "es_cli.o"), "-L" + HERE, "-les_sieve", "-Wl,-rpath,$ORIGIN"])
+    _run(["g++", "-o", CLI, os.path.join(BUILD, "es_cli.o"), "-L" + HERE, "-les_sieve", "-Wl,-rpath,$ORIGIN",
+          "-pthread"])
     if verbose or ptxas_info:
         sys.stdout.write("".join(logs))
     return LIB

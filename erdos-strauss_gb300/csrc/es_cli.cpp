@@ -27,6 +27,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cinttypes>
 #include <ctime>
 #include <cstdio>
@@ -200,7 +204,16 @@ static std::string file_sha256(const char *path) {
 // chunk by chunk, never stored. Round order (sieve/cuda/scan.cu:266-310) needs each chunk to
 // start on a round boundary of every lane: chunks are whole multiples of M * seg integers, so
 // lane l's first position moves by exactly chunk_rounds * seg positions from one chunk to the
-// next, and sorting a chunk's lane-major records by J / seg (stably) gives round, lane, J.
+// next, and a stable counting sort of a chunk's lane-major records by J / seg gives round,
+// lane, J. A producer thread keeps the GPU on the next chunk while this one is sorted,
+// formatted by several threads and hashed in order.
+struct Chunk {
+  es_counters c{};
+  es_records r{nullptr, 0};
+  es_status st = ES_OK;
+  bool last = false;
+};
+
 static int write_meta(es_engine *e, const char *path, u64 lo, u64 hi, u64 M, u64 seg, u64 chunk_rounds,
                       bool round_order, bool emit_surv, u64 shard, u64 nshard, const char *ffile, const char *threads,
                       std::chrono::steady_clock::time_point t0) {
@@ -210,38 +223,100 @@ static int write_meta(es_engine *e, const char *path, u64 lo, u64 hi, u64 M, u64
   es_counters tot{};
   const unsigned __int128 span128 = (unsigned __int128)M * seg * chunk_rounds;
   const u64 span = round_order && span128 < (unsigned __int128)(hi - lo) ? (u64)span128 : hi - lo;
-  std::string chunk_text;
-  char line[160];
-  for (u64 a = lo; a < hi || (a == lo && lo == hi);) {
-    const u64 b = hi - a > span ? a + span : hi;
-    es_counters c;
-    es_records r{};
-    const es_status s = es_run_window(e, a, b, &c, &r);
-    if (s != ES_OK) {
-      fprintf(stderr, "FATAL: %s: %s\n", es_status_str(s), es_last_error(e));
-      return 1;
+  // producer: runs the chunks in order into a queue of at most two
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Chunk> q;
+  bool stop = false;
+  std::thread prod([&] {
+    for (u64 a = lo;;) {
+      const u64 b = hi - a > span ? a + span : hi;
+      Chunk ch;
+      ch.st = es_run_window(e, a, b, &ch.c, &ch.r);
+      ch.last = ch.st != ES_OK || b == hi;
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return q.size() < 2 || stop; });
+      if (stop) { es_free_records(&ch.r); return; }
+      q.push_back(ch);
+      cv.notify_all();
+      if (ch.last) return;
+      a = b;
     }
+  });
+  const unsigned nthr = std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
+  std::vector<es_record> sorted;
+  std::vector<std::string> text(nthr);
+  std::vector<u64> tcerts(nthr);
+  std::vector<std::string> tsurv(nthr);
+  int rc = 0;
+  for (;;) {
+    Chunk ch;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return !q.empty(); });
+      ch = q.front();
+      q.pop_front();
+      cv.notify_all();
+    }
+    if (ch.st != ES_OK) {
+      fprintf(stderr, "FATAL: %s: %s\n", es_status_str(ch.st), es_last_error(e));
+      es_free_records(&ch.r);
+      rc = 1;
+      break;
+    }
+    const es_counters &c = ch.c;
     tot.positions += c.positions; tot.covered += c.covered; tot.sieved += c.sieved; tot.mr += c.mr;
     tot.composite += c.composite; tot.rung += c.rung; tot.direct += c.direct; tot.survivors += c.survivors;
-    if (round_order) std::stable_sort(r.recs, r.recs + r.n, [&](const es_record &x, const es_record &y) {
-      return x.J / seg < y.J / seg;
-    });
-    chunk_text.clear();
-    for (size_t i = 0; i < r.n; ++i) {
-      if (!emit_surv && r.recs[i].kind == ES_REC_SURVIVOR) continue;
-      const size_t k = es_format_record(&r.recs[i], line, sizeof line);
-      chunk_text.append(line, k);
-      if (r.recs[i].kind == ES_REC_SURVIVOR) surv_lines.append(line, k);
-      else ++certs;
+    const es_record *rec = ch.r.recs;
+    const size_t n = ch.r.n;
+    if (round_order && n) {                            // stable counting sort by round
+      u64 rmax = 0;
+      for (size_t i = 0; i < n; ++i) rmax = std::max<u64>(rmax, rec[i].J / seg);
+      std::vector<size_t> start(rmax + 2, 0);
+      for (size_t i = 0; i < n; ++i) ++start[rec[i].J / seg + 1];
+      for (size_t k = 1; k < start.size(); ++k) start[k] += start[k - 1];
+      sorted.resize(n);
+      for (size_t i = 0; i < n; ++i) sorted[start[rec[i].J / seg]++] = rec[i];
+      rec = sorted.data();
     }
-    h.update(chunk_text);
-    es_free_records(&r);
-    if (b == hi) break;
-    a = b;
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nthr; ++t)
+      pool.emplace_back([&, t] {
+        const size_t a = n * t / nthr, b = n * (t + 1) / nthr;
+        std::string &out = text[t];
+        out.clear();
+        out.reserve((b - a) * 80);
+        tcerts[t] = 0;
+        tsurv[t].clear();
+        char line[192];
+        for (size_t i = a; i < b; ++i) {
+          if (!emit_surv && rec[i].kind == ES_REC_SURVIVOR) continue;
+          const size_t k = es_format_record(&rec[i], line, sizeof line);
+          out.append(line, k);
+          if (rec[i].kind == ES_REC_SURVIVOR) tsurv[t].append(line, k);
+          else ++tcerts[t];
+        }
+      });
+    for (std::thread &t : pool) t.join();
+    for (unsigned t = 0; t < nthr; ++t) {
+      h.update(text[t]);
+      certs += tcerts[t];
+      surv_lines += tsurv[t];
+    }
+    es_free_records(&ch.r);
+    if (ch.last) break;
   }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    stop = true;
+    cv.notify_all();
+  }
+  prod.join();
+  for (Chunk &left : q) es_free_records(&left.r);
+  if (rc) return rc;
   char summary[512];
   if (!es_format_summary(e, lo, hi, &tot, summary, sizeof summary)) { fprintf(stderr, "FATAL: SUMMARY\n"); return 1; }
-  const int rc = tot.survivors ? 2 : 0;
+  rc = tot.survivors ? 2 : 0;
   const long wall = (long)std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   char date[32];
   const time_t now = time(nullptr);

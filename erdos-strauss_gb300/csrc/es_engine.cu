@@ -1916,34 +1916,57 @@ es_status es_free_records(es_records *r) {
   return ES_OK;
 }
 
-static int u128_dec(char *out, unsigned long long lo, unsigned long long hi) {
-  unsigned __int128 v = ((unsigned __int128)hi << 64) | lo;
-  char buf[48];
+static char *put_u64(char *o, unsigned long long v) {
+  char b[20];
   int n = 0;
-  if (!v) buf[n++] = '0';
-  while (v) { buf[n++] = (char)('0' + (int)(v % 10)); v /= 10; }
-  for (int i = 0; i < n; ++i) out[i] = buf[n - 1 - i];
-  out[n] = 0;
-  return n;
+  do { b[n++] = (char)('0' + (int)(v % 10)); v /= 10; } while (v);
+  while (n) *o++ = b[--n];
+  return o;
+}
+
+static char *put_u128(char *o, unsigned long long lo, unsigned long long hi) {
+  if (!hi) return put_u64(o, lo);
+  const unsigned __int128 v = ((unsigned __int128)hi << 64) | lo;
+  const unsigned long long P19 = 10000000000000000000ull;
+  const unsigned __int128 q = v / P19;                 // below 2^64 for every u < 2^127
+  unsigned long long r = (unsigned long long)(v % P19);
+  o = q >> 64 ? put_u128(o, (unsigned long long)q, (unsigned long long)(q >> 64)) : put_u64(o, (unsigned long long)q);
+  char b[19];
+  for (int i = 18; i >= 0; --i) { b[i] = (char)('0' + (int)(r % 10)); r /= 10; }
+  memcpy(o, b, 19);
+  return o + 19;
 }
 
 size_t es_format_record(const es_record *r, char *buf, size_t cap) {
   if (!r || !buf) return 0;
-  int k = 0;
+  char line[192];
+  char *o = line;
+  auto put = [&](const char *s, size_t n) { memcpy(o, s, n); o += n; };
   if (r->kind == ES_REC_RUNG) {
-    char u[48];
-    u128_dec(u, r->c, r->d);
-    k = snprintf(buf, cap, "RUNG %llu %llu %llu %s\n", (unsigned long long)r->p, (unsigned long long)r->a,
-                 (unsigned long long)r->b, u);
+    put("RUNG ", 5);
+    o = put_u64(o, r->p); *o++ = ' ';
+    o = put_u64(o, r->a); *o++ = ' ';
+    o = put_u64(o, r->b); *o++ = ' ';
+    o = put_u128(o, r->c, r->d);
   } else if (r->kind == ES_REC_SOLVED) {
-    k = snprintf(buf, cap, "SOLVED %llu %llu %llu %llu %llu\n", (unsigned long long)r->p, (unsigned long long)r->a,
-                 (unsigned long long)r->b, (unsigned long long)r->c, (unsigned long long)r->d);
+    put("SOLVED ", 7);
+    o = put_u64(o, r->p); *o++ = ' ';
+    o = put_u64(o, r->a); *o++ = ' ';
+    o = put_u64(o, r->b); *o++ = ' ';
+    o = put_u64(o, r->c); *o++ = ' ';
+    o = put_u64(o, r->d);
   } else if (r->kind == ES_REC_SURVIVOR) {
-    k = snprintf(buf, cap, "SURVIVOR %llu\n", (unsigned long long)r->p);
+    put("SURVIVOR ", 9);
+    o = put_u64(o, r->p);
   } else {
     return 0;
   }
-  return (k > 0 && (size_t)k < cap) ? (size_t)k : 0;
+  *o++ = '\n';
+  const size_t k = (size_t)(o - line);
+  if (k >= cap) return 0;
+  memcpy(buf, line, k);
+  buf[k] = 0;
+  return k;
 }
 
 size_t es_format_summary(const es_engine *e, uint64_t lo, uint64_t hi, const es_counters *c, char *buf, size_t cap) {

@@ -73,6 +73,22 @@ def test_record_formats(lib):
     assert es_sieve.format_record(_rec(kind=9)) == ""
 
 
+def test_record_formats_random(lib):
+    """Every width of every field, witnesses across the 2^64 and 10^19 boundaries."""
+    import random
+    rng = random.Random(5)
+    us = [0, 1, 9, 10, 2 ** 64 - 1, 2 ** 64, 10 ** 19 - 1, 10 ** 19, 10 ** 19 + 1, 10 ** 38, 2 ** 126 - 1, 2 ** 127 - 1]
+    us += [rng.getrandbits(rng.randint(1, 127)) for _ in range(2000)]
+    for u in us:
+        p, a, b = rng.getrandbits(64), rng.getrandbits(62), rng.randint(1, 255)
+        assert es_sieve.format_record(_rec(kind=1, p=p, a=a, b=b, c=u & (2 ** 64 - 1), d=u >> 64)) == \
+            "RUNG %d %d %d %d\n" % (p, a, b, u)
+    for _ in range(500):
+        v = [rng.getrandbits(rng.randint(1, 64)) for _ in range(5)]
+        assert es_sieve.format_record(_rec(kind=2, p=v[0], a=v[1], b=v[2], c=v[3], d=v[4])) == \
+            "SOLVED %d %d %d %d %d\n" % tuple(v)
+
+
 def test_load_filters_errors(lib, tmp_path):
     m, r, n = C.POINTER(C.c_uint64)(), C.POINTER(C.c_uint64)(), C.c_size_t()
     assert lib.es_load_filters(b"/nonexistent/file", C.byref(m), C.byref(r), C.byref(n)) == es_sieve.ES_ERR_FILTERS
