@@ -38,6 +38,24 @@ def test_sha256_matches_hashlib():
     assert lib.es_sha256_hex(b"x", 1, out, 64) == 0            # no room for the NUL
 
 
+def test_sha256_builtin_backend_matches_hashlib():
+    """The built-in SHA-256 (used when libcrypto is absent) gives the same digests."""
+    import subprocess
+    import sys
+    code = ("import ctypes as C, hashlib, os, sys\n"
+            "lib = C.CDLL(sys.argv[1])\n"
+            "lib.es_sha256_hex.restype = C.c_size_t\n"
+            "lib.es_sha256_hex.argtypes = [C.c_void_p, C.c_size_t, C.c_char_p, C.c_size_t]\n"
+            "for n in (0, 1, 55, 56, 63, 64, 65, 119, 120, 4096, 100003, 1 << 20):\n"
+            "    d = os.urandom(n); out = C.create_string_buffer(65)\n"
+            "    lib.es_sha256_hex(d, n, out, 65)\n"
+            "    assert out.value.decode() == hashlib.sha256(d).hexdigest(), n\n"
+            "print('ok')\n")
+    env = dict(os.environ, ES_SHA256_BUILTIN="1")
+    r = subprocess.run([sys.executable, "-c", code, es_sieve.LIB_PATH], env=env, capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
+
+
 def test_parse_production_meta():
     d = shard_meta.parse_meta(read("metas", "c19_shard_0.meta"))
     assert d["complete"] and d["idx"] == 0 and d["nshards"] == 250 and d["rc"] == 0
