@@ -113,7 +113,10 @@ __device__ __forceinline__ bool cancelled(const volatile int *cancel, int my_k) 
 // n mod d == 0) and its own walks still finish the job alone. No warp ever waits for another.
 constexpr u32 HARD_SLOTS = 32;                 // one per lane of a scanning warp
 #ifndef ES_RHO_POST_STEPS
-#define ES_RHO_POST_STEPS 1024
+#define ES_RHO_POST_STEPS 512
+#endif
+#ifndef ES_HELP_R0
+#define ES_HELP_R0 16
 #endif
 #ifndef ES_HELP_SLEEP_NS
 #define ES_HELP_SLEEP_NS 2000
@@ -141,13 +144,14 @@ __device__ __forceinline__ u32 ld_volatile(const unsigned int *p) { return *(con
 // cstep: the distance to its next one. poll() is called by every lane between batches (warp-
 // uniform) and returns a divisor handed in from outside, ~0 to stop, or 0 to go on.
 template <class Poll>
-__device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep, u64 budget, u32 lane, Poll poll) {
+__device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep, u64 budget, u32 lane, Poll poll,
+                                        u64 r0 = RHO_R0) {
   const u64 y0 = to_mont(2, M);
   u64 c = c0;
   u64 cm = to_mont(c, M);
   u64 y = y0, x = y0, ys = y0, q = M.one;
   u64 steps = 0;
-  for (u64 r = RHO_R0;; r <<= 1) {
+  for (u64 r = r0;; r <<= 1) {
     x = y;
     if (steps + 2 * r > budget) return 0;
     for (u64 i = 0; i < r; ++i) y = addmod(mmul(y, y, M), cm, n);
@@ -258,7 +262,9 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
         ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
       return __shfl_sync(FULL, ext, 0);
     };
-    const u64 d = rho_walk(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll);
+    // a posted cofactor has already outlasted RHO_POST_STEPS of its owner's walks: helpers
+    // start with a longer comparison window
+    const u64 d = rho_walk(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
     if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
       atomicCAS(&hs->found, 0ull, (unsigned long long)d);
     __syncwarp();
