@@ -1508,6 +1508,11 @@ static es_status build_tables(es_engine *e) {
     }
     if ((int)tdp.size() != NTD) return fail(e, ES_ERR_ARG, "trial-division table size");
   }
+  // temporaries of the table build, freed on every return path
+  struct Temps {
+    void *p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~Temps() { for (void *x : p) cudaFree(x); }
+  } temps;
   u64 *d_mods = nullptr, *d_ress = nullptr;
   u32 *d_g = nullptr, *d_inv = nullptr;
   CU(cudaMalloc(&e->d_rho, L * sizeof(u32)));
@@ -1519,9 +1524,13 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
   CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
+  temps.p[0] = d_mods;
   CU(cudaMalloc(&d_ress, std::max<size_t>(nf, 1) * sizeof(u64)));
+  temps.p[1] = d_ress;
   CU(cudaMalloc(&d_g, std::max<size_t>(nf, 1) * sizeof(u32)));
+  temps.p[2] = d_g;
   CU(cudaMalloc(&d_inv, std::max<size_t>(nf, 1) * sizeof(u32)));
+  temps.p[3] = d_inv;
   CU(cudaMemcpy(e->d_rho, rho.data(), L * sizeof(u32), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(e->d_fdesc, fdesc.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(e->d_sdist, sd.data(), sd.size() * sizeof(u32), cudaMemcpyHostToDevice));
@@ -1602,6 +1611,7 @@ static es_status build_tables(es_engine *e) {
     CU(cudaMalloc(&e->d_mdesc, std::max<size_t>(md.size(), 1) * sizeof(MaskDesc)));
     CU(cudaMalloc(&e->d_lfil, std::max<size_t>(lfil.size(), 1) * sizeof(u32)));
     CU(cudaMalloc(&d_fmask, std::max<size_t>(nf, 1) * sizeof(int)));
+    temps.p[4] = d_fmask;
     CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), e->slots[0].stream));
     if (!md.empty()) CU(cudaMemcpy(e->d_mdesc, md.data(), md.size() * sizeof(MaskDesc), cudaMemcpyHostToDevice));
     if (!lfil.empty()) CU(cudaMemcpy(e->d_lfil, lfil.data(), lfil.size() * sizeof(u32), cudaMemcpyHostToDevice));
@@ -1613,12 +1623,10 @@ static es_status build_tables(es_engine *e) {
       CU(cudaGetLastError());
     }
     CU(cudaStreamSynchronize(e->slots[0].stream));
-    cudaFree(d_fmask);
     CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc))));
   }
   CU(cudaStreamSynchronize(e->slots[0].stream));
-  cudaFree(d_mods); cudaFree(d_ress); cudaFree(d_g); cudaFree(d_inv);
   // occupancy of the marking kernel, for the persistent grid
   // The attribute is per function and process-wide: set it to the largest size any engine
   // can ask for (DMAX strides), never to this engine's own size, or a second engine with
@@ -1716,6 +1724,14 @@ static es_status probe(es_engine *e, Slot *sl, size_t count, size_t in_bytes, co
   cudaSetDevice(e->device);
   void *d_in = nullptr;
   std::vector<void *> d_outs(outs.size(), nullptr);
+  struct Release {                                   // the probe's buffers, on every return path
+    void *&in;
+    std::vector<void *> &outs;
+    ~Release() {
+      cudaFree(in);
+      for (void *p : outs) cudaFree(p);
+    }
+  } release{d_in, d_outs};
   (void)out_bytes;
   CU(cudaMalloc(&d_in, std::max<size_t>(in_bytes, 8)));
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMalloc(&d_outs[i], std::max<size_t>(outs[i].second, 8)));
@@ -1730,8 +1746,6 @@ static es_status probe(es_engine *e, Slot *sl, size_t count, size_t in_bytes, co
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMemcpy(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost));
   u32 st = 0;
   CU(cudaMemcpy(&st, sl->d_status, sizeof st, cudaMemcpyDeviceToHost));
-  cudaFree(d_in);
-  for (void *p : d_outs) cudaFree(p);
   (void)count;
   if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
   return ES_OK;
