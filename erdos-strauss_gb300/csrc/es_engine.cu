@@ -1061,6 +1061,7 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
                     std::vector<ShortWin> &shortw) {
   out.resize(n);
   shortw.clear();
+  shortw.reserve(n);
   u64 items = 0;
   const u64 L = e->classes.size(), M = e->M;
   for (size_t i = 0; i < n; ++i) {
@@ -1071,7 +1072,8 @@ static u64 describe(const es_engine *e, const es_window *w, size_t n, std::vecto
     d.Q = q;
     d.lomod = (u32)r;
     const u64 len = d.hi - d.lo;
-    const u64 maxpos = len ? (len - 1) / M + 1 : 0;     // most positions any lane can hold
+    u64 maxpos = 0, rem_;                                // most positions any lane can hold
+    if (len) { divmod_M(e, len - 1, maxpos, rem_); ++maxpos; }
     d.item0 = items;
     d.G = 1; d.lane0 = 0;
     if (maxpos <= e->sched.short_max) {
@@ -1377,7 +1379,7 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
     if (w[i].lo <= floor_)
       return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
     const u64 len = w[i].hi > w[i].lo ? w[i].hi - w[i].lo : 0;
-    if (e->sched.long_split && len && (len - 1) / M + 1 > S) split = true;
+    if (e->sched.long_split && len > S * M) split = true;          // more than S positions per lane
   }
   if (!split) return run_device_windows(e, sl, w, n, schedule, per_window, recs);
   memset(per_window, 0, n * sizeof(es_counters));
@@ -1395,8 +1397,8 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
     dmap.clear();
     while (i < n && dw.size() < PASS_WINDOWS) {
       const u64 lo = w[i].lo, hi = std::max(w[i].lo, w[i].hi);
-      const u64 len = hi - lo, maxpos = len ? (len - 1) / M + 1 : 0;
-      if (!e->sched.long_split || maxpos <= S) {
+      const u64 len = hi - lo;
+      if (!e->sched.long_split || len <= S * M) {
         dw.push_back({lo, hi});
         dmap.push_back({(u32)i, 0});
         ++i;
