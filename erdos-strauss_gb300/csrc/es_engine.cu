@@ -66,13 +66,6 @@ __global__ void k_build_k0(const u32 *__restrict__ rho, u32 L, const u64 *__rest
   K0[idx] = (u16)((d / g) * (u64)invs[f] % s);
 }
 
-// K0T[f][l] = K0[l][f], lanes padded to Lpad with K0_MISS.
-__global__ void k_transpose_k0(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf, u32 Lpad, u16 *__restrict__ K0T) {
-  const u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (u64)nf * Lpad) return;
-  const u32 f = (u32)(idx / Lpad), l = (u32)(idx % Lpad);
-  K0T[idx] = l < L ? K0[(size_t)l * ldk + f] : K0_MISS;
-}
 
 // Clear the progression of every filter in [from, to) over alive[0, n) of one lane.
 template <int BLOCK>
@@ -86,34 +79,6 @@ __device__ __forceinline__ void mark_lane(const u16 *__restrict__ K0row, const u
     int off = (int)k0 - (int)R[fd >> 16];
     if (off < 0) off += (int)s;
     for (u32 j = (u32)off; j < n; j += s) alive[j] = 0;
-  }
-}
-
-// The same for GROUP consecutive lanes at once: one 32-byte load of the transposed table
-// gives filter f's first-hit residue in all 16 lanes; lane g's bytes are
-// alive[g*SEG_SMALL, g*SEG_SMALL + n_g). R0/R1 are the segment-start residues for lanes whose
-// first position sits at K = Q and K = Q + 1 (bmask bit g set for the latter).
-template <int BLOCK>
-__device__ __forceinline__ void mark_group(const u16 *__restrict__ K0T, u32 Lpad, u32 lane_base,
-                                           const u32 *__restrict__ fdesc, const u16 *R0, const u16 *R1,
-                                           u32 bmask, const u32 (&ng)[GROUP], unsigned char *alive, u32 from,
-                                           u32 to) {
-  for (u32 f = from + threadIdx.x; f < to; f += BLOCK) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(K0T + (size_t)f * Lpad + lane_base);
-    const uint4 va = __ldg(src), vb = __ldg(src + 1);
-    const u32 w[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
-    const u32 fd = __ldg(fdesc + f);
-    const int s = (int)(fd & 0xFFFFu);
-    const int r0 = R0[fd >> 16], r1 = R1[fd >> 16];
-    #pragma unroll
-    for (int g = 0; g < (int)GROUP; ++g) {
-      const int k0 = (int)((w[g >> 1] >> (16 * (g & 1))) & 0xFFFFu);
-      if (k0 == K0_MISS) continue;
-      int off = k0 - (((bmask >> g) & 1) ? r1 : r0);
-      if (off < 0) off += s;
-      unsigned char *a = alive + g * SEG_SMALL;
-      for (u32 j = (u32)off; j < ng[g]; j += (u32)s) a[j] = 0;
-    }
   }
 }
 
@@ -249,7 +214,6 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
     u32 ng[GROUP];
     #pragma unroll
     for (int g = 0; g < (int)GROUP; ++g) ng[g] = (g < (int)G) ? it.n[g] : 0;
-    const u32 bmask = it.bmask;
     for (int phase = 0; phase < 2; ++phase) {
       const u32 from = phase ? P.ncov : 0, to = phase ? P.nf : P.ncov;
       if (phase) {                                  // stage B': count survivors of the covers
@@ -259,10 +223,7 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
         c = block_sum<BLOCK>(c, red);
         if (threadIdx.x == 0) atomicAdd(&P.cnt[win].after_covers, (unsigned long long)c);
       }
-      if (G == 1)
-        mark_lane<BLOCK>(P.K0 + (size_t)lane_base * P.ldk, P.fdesc, R0, alive, from, to, ng[0]);
-      else
-        mark_group<BLOCK>(P.K0T, P.Lpad, lane_base, P.fdesc, R0, R1, bmask, ng, alive, from, to);
+      mark_lane<BLOCK>(P.K0 + (size_t)lane_base * P.ldk, P.fdesc, R0, alive, from, to, ng[0]);   // G == 1
       __syncthreads();
     }
     // Compaction: each warp takes 32 consecutive words per step; an inclusive warp scan of
@@ -895,12 +856,12 @@ struct es_engine {
   size_t ncov = 0;
   // marking order: filters sorted by stride within each phase
   std::vector<uint32_t> order;
-  uint32_t nf = 0, ldk = 0, D = 0, Dq = 0, Lpad = 0;
+  uint32_t nf = 0, ldk = 0, D = 0, Dq = 0;
   es_schedule sched{es::SEG_SMALL, 6, 1, {0, 0, 0, 0, 0}};   // es_set_schedule / es_autotune
   int device = 0, sm_count = 0, mark_occupancy = 0;
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
-  es::u16 *d_K0 = nullptr, *d_K0T = nullptr;
+  es::u16 *d_K0 = nullptr;
   // short-window kill masks
   es::u64 *d_mtab = nullptr;
   es::MaskDesc *d_mdesc = nullptr;
@@ -990,8 +951,8 @@ static es_status ensure_capacity(es_engine *e, Slot *sl, size_t nwin, size_t cap
 
 static MarkParams mark_params(const es_engine *e, const Slot *sl) {
   MarkParams P;
-  P.rho = e->d_rho; P.K0 = e->d_K0; P.K0T = e->d_K0T; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
-  P.Qm = sl->d_Qm; P.Lpad = e->Lpad;
+  P.rho = e->d_rho; P.K0 = e->d_K0; P.fdesc = e->d_fdesc; P.sdist = e->d_sdist;
+  P.Qm = sl->d_Qm;
   P.win = sl->d_win; P.queue = reinterpret_cast<u64 *>(sl->d_ctr + 0);
   P.surv = sl->d_surv; P.surv_count = sl->d_ctr + 1; P.cnt = sl->d_cnt;
   P.hdr = sl->d_hdr; P.surv_cap = sl->cap; P.M = e->M;
@@ -1270,15 +1231,19 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
       if (!shortw.empty()) {
         // largest first: the warps of a k_mark_short CTA deal the windows round robin, so the
         // CTA's last window is a small one
-        // keys: descending work in the high bits, the original index (ties in order) below
-        std::vector<u64> key(shortw.size());
-        for (size_t k = 0; k < shortw.size(); ++k) {
+        // a counting sort on the work's binary order of magnitude (largest first, ties in
+        // input order) is all the balance needs
+        const size_t ns = shortw.size();
+        std::vector<uint8_t> mag(ns);
+        u32 start[34] = {0};
+        for (size_t k = 0; k < ns; ++k) {
           const ShortWin &x = shortw[k];
           const u64 work = (u64)(x.lb - x.la) * (x.lq + 1);          // < 2^21
-          key[k] = ((((u64)1 << 24) - 1 - work) << 32) | k;
+          mag[k] = (uint8_t)(32 - __builtin_clz((u32)work | 1u));    // 1 .. 22
+          ++start[33 - mag[k]];
         }
-        std::sort(key.begin(), key.end());
-        for (size_t k = 0; k < key.size(); ++k) sl->h_short[k] = shortw[(u32)key[k]];
+        for (int b = 1; b < 34; ++b) start[b] += start[b - 1];
+        for (size_t k = 0; k < ns; ++k) sl->h_short[start[32 - mag[k]]++] = shortw[k];
       }
       if (!sl->gexec) { s = capture_graph(e, sl); if (s) return s; }
       setup_ms = ms_since(t_start);
@@ -1521,8 +1486,6 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_fdesc, std::max<size_t>(nf, 1) * sizeof(u32)));
   CU(cudaMalloc(&e->d_sdist, std::max<size_t>(sd.size(), 1) * sizeof(u32)));
   CU(cudaMalloc(&e->d_K0, (size_t)L * e->ldk * sizeof(u16)));
-  e->Lpad = (L + GROUP - 1) / GROUP * GROUP;
-  CU(cudaMalloc(&e->d_K0T, (size_t)std::max<size_t>(nf, 1) * e->Lpad * sizeof(u16)));
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
   CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
@@ -1546,11 +1509,6 @@ static es_status build_tables(es_engine *e) {
   k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
                                                                        e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
   CU(cudaGetLastError());
-  if (nf) {
-    const u64 tt = (u64)nf * e->Lpad;
-    k_transpose_k0<<<(unsigned)((tt + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_K0, L, e->ldk, (u32)nf, e->Lpad, e->d_K0T);
-    CU(cudaGetLastError());
-  }
   // Kill masks for short windows: within each phase (covers, then stage-B' primes), the
   // smallest strides get a mask while the per-lane table fits MASK_BYTES_MAX; the filters of
   // the remaining strides are checked one by one from the first-hit table. The masked strides
@@ -1896,7 +1854,7 @@ es_status es_close(es_engine *e) {
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_K0T); cudaFree(e->d_tde);
+  cudaFree(e->d_K0); cudaFree(e->d_tde);
   cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil);
   delete e;
   return ES_OK;

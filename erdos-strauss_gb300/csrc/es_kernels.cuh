@@ -60,7 +60,6 @@ struct RecDev {
 struct MarkParams {
   const u32 *rho;          // [L] lane classes
   const u16 *K0;           // [L][ldk] first hit K mod s per (lane, filter), or K0_MISS
-  const u16 *K0T;          // [nf][Lpad] the same table, lane-contiguous (16-lane vector loads)
   const u32 *fdesc;        // [nf] stride s (low 16 bits) | index of s among distinct strides
   const u32 *sdist;        // [D] distinct strides
   const u16 *Qm;           // [nwin][Dq] (lo / M) mod s_d per window (rows of Dq >= D, 16-byte multiples)
@@ -72,7 +71,7 @@ struct MarkParams {
   const BatchHdr *hdr;     // total_items, nwin
   u64 surv_cap;
   u64 M;
-  u32 L, Lpad, ldk, nf, ncov, D, Dq;
+  u32 L, ldk, nf, ncov, D, Dq;
   u32 r_bytes;             // shared bytes for the stride residues (16-aligned)
 };
 
