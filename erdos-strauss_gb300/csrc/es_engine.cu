@@ -639,10 +639,29 @@ constexpr int RUNG_WARPS = 4;
 #define ES_HELP_BLOCKS_DIV 1
 #endif
 
-// Stage D, one block of RUNG_WARPS warps per prime (block_solve_rung). Blocks take primes
-// from a queue; a block that finds it empty turns its warps into helpers on the hard board
-// (warp_help) until every prime of the run is finished, so that the last, hardest
-// factorizations of a run get the walks of every idle warp instead of one warp's.
+// Stage D. While more primes remain than the grid has warps, every warp takes a prime of its
+// own from a queue and walks its rungs in order (warp_solve_rung: no barrier, no speculative
+// rungs); the last gridDim.x * RUNG_WARPS primes go to whole blocks of RUNG_WARPS warps that
+// try four rungs of one prime at a time (block_solve_rung), so that the run ends on short
+// latencies. A block that finds both queues empty turns its warps into helpers on the hard
+// board (warp_help) until every prime of the run is finished, so that the last, hardest
+// factorizations get more walks than one warp's.
+__device__ __forceinline__ void rung_result(const TailParams &T, const Surv &s, u32 si, bool ok,
+                                            const RungResult &res) {
+  if (ok && !check_rung_cert(s.p, res.A, res.r, res.u)) {
+    atomicOr(T.status, ST_CERT_BAD);                // never emitted
+  } else if (ok) {
+    RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, res.A, res.r, res.u.lo, res.u.hi};
+    put_record(T, rec);
+    atomicAdd(&T.cnt[s.win].rung, 1ull);
+  } else {
+    const unsigned long long k = atomicAdd(T.direct_count, 1ull);
+    if (k < T.cap) T.direct[k] = si;
+  }
+  __threadfence();
+  atomicAdd(T.rung_done, 1ull);
+}
+
 __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T, int no_rung) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
@@ -652,10 +671,25 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
   __shared__ RungResult res;
   __shared__ unsigned long long next;
   const u64 n = min((u64)*T.prime_count, T.cap);
+  const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   HardBoard B;
   B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
+  const u64 tail = min(n, (u64)gridDim.x * RUNG_WARPS);
+  const u64 nw = n - tail;                           // primes [0, nw): a warp each
   for (;;) {
-    if (threadIdx.x == 0) next = atomicAdd(T.rung_next, 1ull);
+    u64 i = 0;
+    if (lane == 0) i = atomicAdd(T.rung_next_warp, 1ull);
+    i = __shfl_sync(0xFFFFFFFFu, i, 0);
+    if (i >= nw) break;
+    const u32 si = T.primes[i];
+    const Surv s = T.surv[si];
+    const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tde, T.status, F[w], D[w], rho_slot + w, &slot[w], &B);
+    if (lane == 0) rung_result(T, s, si, ok, slot[w]);
+    __syncwarp();
+  }
+  __syncthreads();
+  for (;;) {                                          // primes [nw, n): a block each
+    if (threadIdx.x == 0) next = nw + atomicAdd(T.rung_next, 1ull);
     __syncthreads();
     const u64 i = next;
     if (i >= n) break;
@@ -663,27 +697,14 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
     const Surv s = T.surv[si];
     const bool ok = !no_rung &&
                     block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B);
-    if (threadIdx.x == 0) {
-      if (ok && !check_rung_cert(s.p, res.A, res.r, res.u)) {
-        atomicOr(T.status, ST_CERT_BAD);            // never emitted
-      } else if (ok) {
-        RecDev rec{ES_REC_RUNG, s.win, s.lane, 0, s.J, s.p, res.A, res.r, res.u.lo, res.u.hi};
-        put_record(T, rec);
-        atomicAdd(&T.cnt[s.win].rung, 1ull);
-      } else {
-        const unsigned long long k = atomicAdd(T.direct_count, 1ull);
-        if (k < T.cap) T.direct[k] = si;
-      }
-      __threadfence();
-      atomicAdd(T.rung_done, 1ull);
-    }
+    if (threadIdx.x == 0) rung_result(T, s, si, ok, res);
     __syncthreads();
   }
   // Helpers come from the first help_blocks blocks only (one per SM): the walks of a hard
   // cofactor progress at the issue rate their sub-partition gives them, so helpers beyond
   // one warp per scheduler would only split that rate over more walks, and the expected wait
   // for the first collision grows with the square root of the number of walks sharing it.
-  if (!no_rung && blockIdx.x < T.help_blocks) warp_help(B, threadIdx.x & 31);
+  if (!no_rung && blockIdx.x < T.help_blocks) warp_help(B, lane);
 }
 
 __global__ void k_direct(const TailParams T) {
@@ -818,7 +839,8 @@ struct Slot {
   RecDev *d_recs = nullptr;
   size_t cap = 0;
   unsigned long long *d_ctr = nullptr;  // [0] queue [1] surv [2] prime [3] direct [4] rec [5] cand
-                                      // [6] rung queue [7] rungs done [8] help sessions, board at [16]
+                                      // [6] rung queue (blocks) [7] rungs done [8] help sessions
+                                      // [9] rung queue (warps), board at [16]
   u32 *d_status = nullptr;
   es_timing_t timing{};
   std::mutex mu;                        // one run at a time per slot
@@ -970,6 +992,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.direct = sl->d_direct; T.direct_count = sl->d_ctr + 3;
   T.recs = sl->d_recs; T.rec_count = sl->d_ctr + 4;
   T.rung_next = sl->d_ctr + 6; T.rung_done = sl->d_ctr + 7; T.help_sessions = sl->d_ctr + 8;
+  T.rung_next_warp = sl->d_ctr + 9;
   T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
   T.help_blocks = (u32)(e->sm_count * ES_HELP_BLOCKS_PER_SM / ES_HELP_BLOCKS_DIV);
   T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;

@@ -128,7 +128,8 @@ struct TailParams {
   const TdEntry *tde;
   u32 *status;
   u64 cap;                 // capacity of surv/primes/direct/recs
-  unsigned long long *rung_next;      // k_rung's prime queue head
+  unsigned long long *rung_next;      // k_rung's prime queue head, whole blocks (the tail)
+  unsigned long long *rung_next_warp; // k_rung's prime queue head, one warp per prime
   unsigned long long *rung_done;      // primes k_rung has finished
   unsigned long long *help_sessions;  // helping sessions started on the hard board
   struct HardSlot *board;             // [HARD_SLOTS] cofactors whose rho takes long

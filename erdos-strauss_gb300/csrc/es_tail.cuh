@@ -430,6 +430,34 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
 
 struct RungResult { u64 A; u32 r, k; U128 u; };
 
+// The rung walk of one prime by one warp, rung after rung (solve_rung3,
+// sieve/rung_scan3.cpp:578-603, in its own order): the throughput form of block_solve_rung
+// below, for while there are more primes than warps. Returns true in every lane when a rung
+// certifies p, with the result in *out (written by lane 0).
+__device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac &F,
+                                       DPWarp &D, volatile u64 *rho_slot, RungResult *out,
+                                       const HardBoard *board = nullptr) {
+  const u32 lane = threadIdx.x & 31;
+  const u32 pm4 = (u32)(p & 3);
+  const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
+  for (u32 k = 0;; ++k) {
+    const u32 r = r0 + 4 * k;
+    if (r > RCAP) return false;
+    const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
+    if (!A) continue;
+    const u32 qm = (u32)(((p % r) * (A % r)) % r);
+    if (r > 1 && gcd64(qm, r) != 1) continue;
+    const u32 target = qm ? r - qm : 0;
+    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board)) return false;
+    const U128 q{p * A, __umul64hi(p, A)};
+    const U128 u = warp_min_div_res(p, F, q, r, target, D, lane);
+    if (u.lo == 0 && u.hi == 0) continue;
+    if (lane == 0) *out = RungResult{A, r, k, u};
+    __syncwarp();
+    return true;
+  }
+}
+
 // The rung walk of one prime by a block of W warps (solve_rung3, sieve/rung_scan3.cpp:
 // 578-603). Warp w takes rung indices k = w, w+W, ... (r = r0 + 4k) in increasing order and
 // stops once k passes the best certifying index found by any warp. Returns true in every

@@ -149,6 +149,26 @@ def test_batch_equals_windows_run_alone():
         assert e.stream(*wins[i]) == blocks[i]
 
 
+def test_many_primes_warp_and_block_phases():
+    """A 10^12-integer window at 10^17 has about 9 K primes, more than the stage-D grid has
+    warps: most take the warp-per-prime phase and the last ones the block phase. The
+    records must equal those of the same window cut into pieces small enough that all their
+    primes go to the block phase."""
+    e = engine()
+    lo, hi = 10 ** 17 + 99991, 10 ** 17 + 99991 + 10 ** 12
+    c, r = e.run_window(lo, hi)
+    assert c["rung"] > 8000
+    step = (hi - lo) // 8
+    got, n_rung = [], 0
+    for i in range(8):
+        a, b = lo + i * step, (lo + (i + 1) * step if i < 7 else hi)
+        pc, pr = e.run_window(a, b)                 # about 1.1 K primes each: block phase only
+        n_rung += pc["rung"]
+        got += [(int(x["p"]), int(x["a"]), int(x["b"]), int(x["c"]), int(x["d"])) for x in pr]
+    assert n_rung == c["rung"]
+    assert sorted(got) == sorted((int(x["p"]), int(x["a"]), int(x["b"]), int(x["c"]), int(x["d"])) for x in r)
+
+
 def test_repeat_runs_are_identical():
     c = workloads.c3()
     e = engine()

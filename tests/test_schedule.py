@@ -74,7 +74,7 @@ def test_autotune_picks_a_candidate_and_keeps_results(eng):
     assert eng.schedule() == chosen
     c, r = eng.run_batch(wins)
     assert c == before_c and r.tobytes() == before_r.tobytes()
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6)
+    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=1)
 
 
 def test_schedule_refusals(eng):
