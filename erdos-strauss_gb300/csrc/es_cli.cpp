@@ -18,7 +18,10 @@
 //                      64) so no chunk holds more than its own records; --order lane emits
 //                      rung_scan3's order and runs the shard as one window. And
 //   rung_scan3_gb300 --batch FILE [flags]   one "LO HI" per line, each window's stream and
-//                                           SUMMARY in file order, run as one batch.
+//                                           SUMMARY in file order, run as one batch;
+//   rung_scan3_gb300 --serve FILE|- [flags] the same lines read as they arrive (stdin for
+//                                           "-"), each window submitted at once and printed in
+//                                           input order as soon as it is done.
 // stdout carries only the certificate stream and SUMMARY; everything else goes to stderr.
 // Exit status: 0 no survivors, 2 survivors present, 1 refusal or error.
 #include "../../include/es_sieve.h"
@@ -52,6 +55,61 @@ static void print_records(FILE *out, const es_record *r, size_t n, bool emit_sur
     if (buf.size() > (1 << 20)) { fwrite(buf.data(), 1, buf.size(), out); buf.clear(); }
   }
   fwrite(buf.data(), 1, buf.size(), out);
+}
+
+// --serve: windows ("LO HI" per line) are read from FILE or standard input and submitted as
+// they are read (es_submit: the engine batches whatever is queued whenever one of its
+// serving streams frees up); each window's stream and SUMMARY go to stdout in input order as
+// soon as it and every window before it are done. A full queue (ES_ERR_BUSY) makes the
+// reader wait for the oldest window first.
+static int serve_stream(es_engine *e, const char *path, const es_info_t &info, bool emit_surv) {
+  FILE *in = strcmp(path, "-") ? fopen(path, "r") : stdin;
+  if (!in) { fprintf(stderr, "FATAL: cannot open %s\n", path); return 1; }
+  struct Pending { es_window w; uint64_t t; };
+  std::deque<Pending> q;
+  u64 survivors = 0;
+  int rc = 0;
+  auto finish_front = [&](int timeout_ms) -> es_status {   // prints the oldest window if done
+    es_counters c;
+    es_records r{};
+    const es_status st = es_poll(e, q.front().t, &c, &r, timeout_ms);
+    if (st == ES_ERR_TIMEOUT) return st;
+    if (st != ES_OK) { fprintf(stderr, "FATAL: %s: %s\n", es_status_str(st), es_last_error(e)); return st; }
+    print_records(stdout, r.recs, r.n, emit_surv);
+    char line[512];
+    fputs(es_format_summary(e, q.front().w.lo, q.front().w.hi, &c, line, sizeof line) ? line : "SUMMARY ?\n", stdout);
+    fflush(stdout);
+    survivors += c.survivors;
+    es_free_records(&r);
+    q.pop_front();
+    return ES_OK;
+  };
+  unsigned long long a, b;
+  while (rc == 0 && fscanf(in, "%llu %llu", &a, &b) == 2) {
+    if (b > info.ceiling || a <= info.floor) {
+      fprintf(stderr, "FATAL: window [%llu, %llu) outside (%llu, %llu]\n", a, b, (unsigned long long)info.floor,
+              (unsigned long long)info.ceiling);
+      rc = 1;
+      break;
+    }
+    const es_window w{a, b};
+    uint64_t t = 0;
+    es_status st;
+    while ((st = es_submit(e, &w, 1, &t)) == ES_ERR_BUSY && !q.empty())
+      if (finish_front(-1) != ES_OK) { rc = 1; break; }
+    if (rc) break;
+    if (st != ES_OK) { fprintf(stderr, "FATAL: %s: %s\n", es_status_str(st), es_last_error(e)); rc = 1; break; }
+    q.push_back({w, t});
+    while (!q.empty()) {                             // print whatever is already done, in order
+      const es_status f = finish_front(0);
+      if (f == ES_ERR_TIMEOUT) break;
+      if (f != ES_OK) { rc = 1; break; }
+    }
+  }
+  while (rc == 0 && !q.empty())
+    if (finish_front(-1) != ES_OK) rc = 1;
+  if (in != stdin) fclose(in);
+  return rc ? rc : (survivors ? 2 : 0);
 }
 
 static int open_engine(es_config &cfg, es_engine **e) {
@@ -351,6 +409,7 @@ int main(int argc, char **argv) {
     return 0;
   }
   const bool batch = argc >= 3 && !strcmp(argv[1], "--batch");
+  const bool serve = argc >= 3 && !strcmp(argv[1], "--serve");
   if (argc < 3) {
     fprintf(stderr,
             "usage: %s LO HI [--mmax N] [--wheel M] [--seg N] [--threads N]\n"
@@ -358,14 +417,15 @@ int main(int argc, char **argv) {
             "                 [--no-emit-survivors] [--device N] [--profile] [--autotune]\n"
             "                 [--meta FILE [--order round|lane] [--chunk-rounds R]]\n"
             "       %s --batch FILE [flags]\n"
+            "       %s --serve FILE|- [flags]\n"
             "       %s --verify | --dump-classes [--wheel M] | --check-direct LO N | --check-factor [N]\n"
             "GB300 verification sieve: certifies 4/p solvable for every prime in [LO, HI),\n"
             "byte for byte the record of the reference rung_scan3.\n",
-            argv[0], argv[0], argv[0]);
+            argv[0], argv[0], argv[0], argv[0]);
     return 1;
   }
   u64 lo = 0, hi = 0;
-  if (!batch) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
+  if (!batch && !serve) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
   u64 M = 2042040, mmax = 10000, seg = 262144, shard = 0, nshard = 1, sieve_p = 0;
   bool emit_surv = true, profile = false, no_rung = false, autotune = false, round_order = true;
   const char *ffile = nullptr, *meta = nullptr, *threads = "1";
@@ -399,8 +459,11 @@ int main(int argc, char **argv) {
   if (!seg) seg = 262144;
   if (nshard == 0) nshard = 1;
   if (!chunk_rounds) chunk_rounds = 64;
-  if (meta && batch) { fprintf(stderr, "FATAL: --meta writes one shard's record; it does not take --batch\n"); return 1; }
-  if (!batch && nshard > 1) {                 // ceil-span tiling, sieve/rung_scan3.cpp:1022-1027
+  if (meta && (batch || serve)) {
+    fprintf(stderr, "FATAL: --meta writes one shard's record; it does not take --batch or --serve\n");
+    return 1;
+  }
+  if (!batch && !serve && nshard > 1) {       // ceil-span tiling, sieve/rung_scan3.cpp:1022-1027
     const u64 span = (hi - lo + nshard - 1) / nshard;
     const u64 a = lo + shard * span, b = std::min(hi, a + span);
     lo = a; hi = std::max(a, b);
@@ -429,6 +492,11 @@ int main(int argc, char **argv) {
   es_info(e, &info);
   if (!info.pinned) fprintf(stderr, "[rung_scan3_gb300] WARNING: no pinned digest for M=%llu -- running UNPINNED\n",
                             (unsigned long long)M);
+  if (serve) {
+    const int rc = serve_stream(e, argv[2], info, emit_surv);
+    es_close(e);
+    return rc;
+  }
   std::vector<es_window> wins;
   if (batch) {
     FILE *fp = fopen(argv[2], "r");

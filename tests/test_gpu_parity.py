@@ -324,3 +324,15 @@ def test_device_certificate_check_on_reference_records_and_planted_mistakes():
     s = good[:4].copy()
     s["kind"] = es_sieve.ES_REC_SURVIVOR
     assert not engine().check_records(s).any()
+
+
+def test_cli_serve_streams_each_window_in_input_order(tmp_path):
+    """rung_scan3_gb300 --serve -: windows read from stdin are submitted as they arrive and
+    printed in input order; the output is the batch sample's golden record."""
+    import subprocess
+    wins = [tuple(int(x) for x in ln.split()) for ln in read("gen", "batch48.windows").splitlines()]
+    stdin = "".join("%d %d\n" % w for w in wins)
+    r = subprocess.run([es_sieve.CLI_PATH, "--serve", "-", "--filters", golden("filters", GPU_TABLE)],
+                       input=stdin, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-500:]
+    assert r.stdout == read("gen", "batch48.out")
