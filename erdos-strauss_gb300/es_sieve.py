@@ -241,7 +241,7 @@ class Engine:
 
     def run_batch(self, windows, schedule=ES_SCHED_PERSISTENT, records=True):
         n = len(windows)
-        w = (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        w = self.make_windows(windows)
         c = (Counters * max(n, 1))()
         r = Records()
         self._check(self.lib.es_run_batch(self.h, w, n, schedule, c, C.byref(r) if records else None))
@@ -251,8 +251,12 @@ class Engine:
     # make_counters), records freed here; returns the record count.
     @staticmethod
     def make_windows(windows):
-        n = len(windows)
-        return (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        """A ctypes es_window array from (lo, hi) pairs, built through numpy (no per-window
+        Python objects)."""
+        a = np.zeros((max(len(windows), 1), 2), dtype=np.uint64)
+        if len(windows):
+            a[:len(windows)] = np.asarray(windows, dtype=np.uint64).reshape(-1, 2)
+        return (Window * len(a)).from_buffer_copy(a.tobytes())
 
     @staticmethod
     def make_counters(n):
@@ -285,7 +289,7 @@ class Engine:
     def autotune(self, windows, repeats=2):
         """Time the candidate schedules on these windows, keep the fastest; returns it."""
         n = len(windows)
-        w = (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        w = self.make_windows(windows)
         sc = Schedule()
         self._check(self.lib.es_autotune(self.h, w, n, repeats, C.byref(sc)))
         return sc.as_dict()
@@ -294,7 +298,7 @@ class Engine:
     def submit(self, windows):
         """Queue windows; returns a ticket. Raises EsError(ES_ERR_BUSY) when admission is refused."""
         n = len(windows)
-        w = (Window * max(n, 1))(*[Window(int(a), int(b)) for a, b in windows])
+        w = self.make_windows(windows)
         t = C.c_uint64()
         self._check(self.lib.es_submit(self.h, w, n, C.byref(t)))
         return t.value
