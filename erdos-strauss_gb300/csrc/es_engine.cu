@@ -683,7 +683,8 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
     if (i >= nw) break;
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
-    const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tde, T.status, F[w], D[w], rho_slot + w, &slot[w], &B);
+    const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tde, T.status, F[w], D[w], rho_slot + w, &slot[w], &B,
+                                                T.rho_budget);
     if (lane == 0) rung_result(T, s, si, ok, slot[w]);
     __syncwarp();
   }
@@ -696,7 +697,8 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T,
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
     const bool ok = !no_rung &&
-                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B);
+                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B,
+                                                 T.rho_budget);
     if (threadIdx.x == 0) rung_result(T, s, si, ok, res);
     __syncthreads();
   }
@@ -748,7 +750,7 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
 }
 __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
-                                                               const TdEntry *tde, u32 *status) {
+                                                               const TdEntry *tde, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -756,7 +758,8 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_probe_rung(const u64 *p,
   __shared__ RungResult slot[RUNG_WARPS];
   __shared__ RungResult res;
   for (u64 i = blockIdx.x; i < count; i += gridDim.x) {
-    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res);
+    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res, nullptr,
+                                           rho_budget);
     if (threadIdx.x == 0) {
       if (ok && !check_rung_cert(p[i], res.A, res.r, res.u)) { atomicOr(status, ST_CERT_BAD); ok = false; }
       found[i] = ok;
@@ -778,14 +781,14 @@ __global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned ch
 }
 // The production factorization (warp_factor), one warp per value; primes sorted ascending.
 __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *ex, unsigned char *k,
-                               const u32 *tdp, const TdEntry *tde, u32 *status) {
+                               const u32 *tdp, const TdEntry *tde, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[4];
   __shared__ u64 rho_slot[4];
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const u64 warps = (u64)gridDim.x * blockDim.x / 32;
   for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < count; i += warps) {
     WarpFac &f = F[w];
-    const bool ok = warp_factor(n[i], f, tdp, tde, status, lane, rho_slot + w);
+    const bool ok = warp_factor(n[i], f, tdp, tde, status, lane, rho_slot + w, nullptr, 0, nullptr, rho_budget);
     if (lane == 0) {
       const int kk = ok ? f.k : 0;
       for (int a = 1; a < kk; ++a)
@@ -880,6 +883,7 @@ struct es_engine {
   std::vector<uint32_t> order;
   uint32_t nf = 0, ldk = 0, D = 0, Dq = 0;
   es_schedule sched{es::SEG_SMALL, 6, 1, {0, 0, 0, 0, 0}};   // es_set_schedule / es_autotune
+  es::u64 rho_budget = es::WARP_RHO_STEPS;                      // ES_FLAG_TEST_RHO_BUDGET: 64
   int device = 0, sm_count = 0, mark_occupancy = 0;
   // resident device tables
   es::u32 *d_rho = nullptr, *d_fdesc = nullptr, *d_sdist = nullptr, *d_tdp = nullptr;
@@ -995,6 +999,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.rung_next_warp = sl->d_ctr + 9;
   T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
   T.help_blocks = (u32)(e->sm_count * ES_HELP_BLOCKS_PER_SM / ES_HELP_BLOCKS_DIV);
+  T.rho_budget = e->rho_budget;
   T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;
   T.cap = sl->cap;
   return T;
@@ -1793,6 +1798,7 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   e->sieve_p = cfg->sieve_p;
   e->device = cfg->device;
   e->flags = cfg->flags;
+  if (e->flags & ES_FLAG_TEST_RHO_BUDGET) e->rho_budget = 64;
   if (e->M < 2 || e->M > 0x7FFFFFFFull) { g_open_error = "wheel modulus must be below 2^31"; delete e; return ES_ERR_ARG; }
   const std::vector<Cover> covers = gen_covers(e->mmax);
   const Wheel w = build_wheel(e->M, gen_wheel_covers(e->M), gen_ucerts(UCERT_RMAX, UCERT_UMAX));
@@ -2092,7 +2098,7 @@ es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_
                [&](void *in, std::vector<void *> &o) {
                  k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->slots[0].stream>>>((const u64 *)in, count, (RecDev *)o[0],
                                                                      (unsigned char *)o[1], e->d_tdp, e->d_tde,
-                                                                     e->slots[0].d_status);
+                                                                     e->slots[0].d_status, e->rho_budget);
                });
 }
 
@@ -2114,7 +2120,8 @@ es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_
                [&](void *in, std::vector<void *> &o) {
                  k_probe_factor<<<e->sm_count * 4, 128, 0, e->slots[0].stream>>>((const u64 *)in, count, (u64 *)o[0],
                                                                        (unsigned char *)o[1], (unsigned char *)o[2],
-                                                                       e->d_tdp, e->d_tde, e->slots[0].d_status);
+                                                                       e->d_tdp, e->d_tde, e->slots[0].d_status,
+                                                                       e->rho_budget);
                });
 }
 

@@ -134,6 +134,7 @@ struct TailParams {
   unsigned long long *help_sessions;  // helping sessions started on the hard board
   struct HardSlot *board;             // [HARD_SLOTS] cofactors whose rho takes long
   u32 help_blocks;                    // k_rung blocks [0, help_blocks) help on the board
+  u64 rho_budget;                     // Brent steps per lane before a factorization gives up
 };
 
 }  // namespace es

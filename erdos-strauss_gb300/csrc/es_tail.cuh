@@ -187,7 +187,7 @@ __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep,
 }
 
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
-                               int my_k = 0, const HardBoard *board = nullptr) {
+                               int my_k = 0, const HardBoard *board = nullptr, u64 budget = WARP_RHO_STEPS) {
   const Mont M = mont_init(n);
   int slot = -1;                                   // the board slot this warp posted n in
   auto poll = [&](u64 steps) -> u64 {
@@ -212,7 +212,7 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
     }
     return __shfl_sync(FULL, ext, 0);
   };
-  const u64 f = rho_walk(n, M, 1 + lane, 32, WARP_RHO_STEPS, lane, poll);
+  const u64 f = rho_walk(n, M, 1 + lane, 32, budget, lane, poll);
   if (lane == 0 && slot >= 0 && slot < (int)HARD_SLOTS) {  // take n off the board
     atomicExch(&board->slot[slot].state, 1u);
     board->slot[slot].n = 0;
@@ -276,7 +276,7 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
 __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
                                    u32 *status, u32 lane, volatile u64 *rho_slot,
                                    const volatile int *cancel = nullptr, int my_k = 0,
-                                   const HardBoard *board = nullptr) {
+                                   const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
   if (n <= 1) return true;
@@ -357,7 +357,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
         const u64 s = isqrt64(v);
         if (s * s == v) { wf_add(F, s, 2, lane); continue; }
-        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board);
+        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board, rho_budget);
         if (d == 0) return false;                  // budget (status set) or cancelled
         if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
         stack[sp++] = d;
@@ -436,7 +436,7 @@ struct RungResult { u64 A; u32 r, k; U128 u; };
 // certifies p, with the result in *out (written by lane 0).
 __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac &F,
                                        DPWarp &D, volatile u64 *rho_slot, RungResult *out,
-                                       const HardBoard *board = nullptr) {
+                                       const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
   const u32 lane = threadIdx.x & 31;
   const u32 pm4 = (u32)(p & 3);
   const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
@@ -448,7 +448,7 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board)) return false;
+    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board, rho_budget)) return false;
     const U128 q{p * A, __umul64hi(p, A)};
     const U128 u = warp_min_div_res(p, F, q, r, target, D, lane);
     if (u.lo == 0 && u.hi == 0) continue;
@@ -465,7 +465,7 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde
 template <int W>
 __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
                                  volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out,
-                                 const HardBoard *board = nullptr) {
+                                 const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) *best_k = 0x7FFFFFFF;
   if (lane == 0) slot[w].k = 0x7FFFFFFF;
@@ -482,7 +482,7 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *td
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k, board)) break;
+    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k, board, rho_budget)) break;
     const U128 q{p * A, __umul64hi(p, A)};
     const U128 u = warp_min_div_res(p, F[w], q, r, target, D[w], lane);
     if (u.lo == 0 && u.hi == 0) continue;

@@ -161,14 +161,15 @@ def format_record(rec):
 
 
 class Engine:
-    def __init__(self, wheel=2042040, mmax=10000, sieve_p=0, filters=None, device=0, no_rung=False, mem_budget=0):
+    def __init__(self, wheel=2042040, mmax=10000, sieve_p=0, filters=None, device=0, no_rung=False, mem_budget=0,
+                 test_rho_budget=False):
         """filters: None (the generated default set), a filter-file path, or (mods, ress)."""
         self.lib = load_library()
         if isinstance(filters, str):
             filters = load_filters(filters)
         cfg = Config()
         cfg.wheel_M, cfg.mmax, cfg.sieve_p, cfg.device = wheel, mmax, sieve_p, device
-        cfg.flags = 1 if no_rung else 0
+        cfg.flags = (1 if no_rung else 0) | (2 if test_rho_budget else 0)
         cfg.mem_budget = mem_budget
         self._keep = None
         if filters is not None:

@@ -58,6 +58,11 @@ typedef struct {
 /* Test hook of the frozen reference sieve (cover_scan --no-rung, sieve/cover_scan.cpp:395,
  * :431): skip stage D so that every prime goes to the direct search. */
 #define ES_FLAG_NO_RUNG 1u
+/* Test hook for the device-failure path: Brent's rho gives up after 64 steps per lane instead
+ * of 2^24, so a cofactor with two large prime factors exhausts it; the run then fails with
+ * ES_ERR_DEVICE_STATUS ("rho-budget") instead of emitting anything, and the engine stays
+ * usable. Never set in production. */
+#define ES_FLAG_TEST_RHO_BUDGET 2u
 
 /* SUMMARY counters (Scan3Stats, sieve/rung_scan3.cpp:651-660). */
 typedef struct {

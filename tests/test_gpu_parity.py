@@ -336,3 +336,24 @@ def test_cli_serve_streams_each_window_in_input_order(tmp_path):
                        input=stdin, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-500:]
     assert r.stdout == read("gen", "batch48.out")
+
+
+def test_device_failure_surfaces_as_status_and_engine_stays_usable():
+    """With the test hook that cuts Brent's rho to 64 steps, a semiprime of two 31-bit primes
+    cannot be split: the probe and a window that needs it fail with ES_ERR_DEVICE_STATUS
+    ("rho-budget"), nothing wrong is emitted, and the same engine keeps working."""
+    e = es_sieve.Engine(wheel=2042040, filters=golden("filters", GPU_TABLE), test_rho_budget=True)
+    try:
+        semi = 2147483659 * 2147483693
+        with pytest.raises(es_sieve.EsError) as ex:
+            e.factor([semi])
+        assert ex.value.status == es_sieve.ES_ERR_DEVICE_STATUS and "rho-budget" in str(ex.value)
+        assert e.factor([2 ** 40 * 3 ** 5]) == [oracle.factor(2 ** 40 * 3 ** 5)]
+        c = workloads.c3()
+        with pytest.raises(es_sieve.EsError) as ex:
+            e.run_window(c["lo"], c["hi"])
+        assert ex.value.status == es_sieve.ES_ERR_DEVICE_STATUS
+        assert list(e.is_prime([2 ** 61 - 1, 2 ** 61 + 1])) == [True, False]
+    finally:
+        e.close()
+    assert engine().stream(workloads.c3()["lo"], workloads.c3()["hi"]) == read("gen", "c3_gpu.out")
