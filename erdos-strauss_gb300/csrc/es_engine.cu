@@ -557,16 +557,14 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
         const u32 b[SHORT_LANES] = {(pj >> 18) & 1u, (pj >> 19) & 1u};
         const u32 nmax = max(n[0], n[1]);
         const WinRef R{wi, x.x, x.y, j};
-        switch ((nmax + 31) >> 5) {
-          case 1: short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 2: short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 3: short_segments<3>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 4: short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 5: short_segments<5>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 6: short_segments<6>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          case 7: short_segments<7>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-          default: short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane); break;
-        }
+        // chunks per lane; one chunk is by far the commonest case, so it is tested first.
+        const u32 nc = (nmax + 31) >> 5;
+        // four instantiations (1, 2, 4, 8 chunks) measured faster than one per chunk count: the
+        // kernel's code stays small enough for the instruction cache
+        if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        else if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
       }
     }
     __syncthreads();
