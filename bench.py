@@ -40,10 +40,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
 METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch: one ncu
-# capture of this kernel on this workload (dram__bytes_read.sum 89.28 MB +
-# dram__bytes_write.sum 3.42 MB); scaled by the mask bytes when another batch size is run.
-MARK_SHORT_TRAFFIC_4096 = 89.275136e6 + 3.423232e6
-MARK_SHORT_INST_4096 = 906350355             # smsp__inst_executed.sum of the same capture
+# capture of this kernel on this workload (dram__bytes_read.sum 89.26 MB +
+# dram__bytes_write.sum 3.67 MB); scaled by the mask bytes when another batch size is run.
+MARK_SHORT_TRAFFIC_4096 = 89.263872e6 + 3.667968e6
+MARK_SHORT_INST_4096 = 873845259             # smsp__inst_executed.sum of the same capture
 
 
 def parse():
