@@ -629,7 +629,10 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
   if (k < T.cap) T.recs[k] = r;
 }
 
-constexpr int RUNG_WARPS = 4;
+#ifndef ES_RUNG_WARPS
+#define ES_RUNG_WARPS 4
+#endif
+constexpr int RUNG_WARPS = ES_RUNG_WARPS;
 #ifndef ES_HELP_BLOCKS_PER_SM
 #define ES_HELP_BLOCKS_PER_SM 1
 #endif
@@ -660,7 +663,7 @@ __device__ __forceinline__ void rung_result(const TailParams &T, const Surv &s, 
   atomicAdd(T.rung_done, 1ull);
 }
 
-__global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_rung(const TailParams T, int no_rung) {
+__global__ void __launch_bounds__(RUNG_WARPS * 32, 16 / RUNG_WARPS) k_rung(const TailParams T, int no_rung) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -746,7 +749,7 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
     if (lane == 0) out[i] = pr ? 1 : 0;
   }
 }
-__global__ void __launch_bounds__(RUNG_WARPS * 32, 4) k_probe_rung(const u64 *p, u64 count, RecDev *out,
+__global__ void __launch_bounds__(RUNG_WARPS * 32, 16 / RUNG_WARPS) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
                                                                const TdEntry *tde, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[RUNG_WARPS];
