@@ -563,8 +563,12 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
         // kernel's code stays small enough for the instruction cache
         if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
         else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
-        else if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
-        else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        else if constexpr (SEG_SMALL > 128) {
+          if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+          else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        } else if constexpr (SEG_SMALL > 64) {
+          short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        }
       }
     }
     __syncthreads();
@@ -1373,7 +1377,8 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
     if (w[i].lo <= floor_)
       return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
     const u64 len = w[i].hi > w[i].lo ? w[i].hi - w[i].lo : 0;
-    if (e->sched.long_split && len > S * M) split = true;          // more than S positions per lane
+    // more than S positions per lane; the plain schedule keeps one launch sequence per window
+    if (e->sched.long_split && schedule == ES_SCHED_PERSISTENT && len > S * M) split = true;
   }
   if (!split) return run_device_windows(e, sl, w, n, schedule, per_window, recs);
   memset(per_window, 0, n * sizeof(es_counters));
@@ -1996,7 +2001,8 @@ es_status es_get_schedule(const es_engine *e, es_schedule *o) {
 
 es_status es_set_schedule(es_engine *e, const es_schedule *s) {
   if (!e || !s) return ES_ERR_ARG;
-  if (s->short_max < 1 || s->short_max > es::SEG_SMALL) return fail(e, ES_ERR_ARG, "short_max must be in 1..256");
+  if (s->short_max < 1 || s->short_max > es::SEG_SMALL)
+    return fail(e, ES_ERR_ARG, "short_max must be in 1.." + std::to_string(es::SEG_SMALL));
   if (s->rung_blocks_per_sm < 1 || s->rung_blocks_per_sm > 16)
     return fail(e, ES_ERR_ARG, "rung_blocks_per_sm must be in 1..16");
   if (s->long_split > 1) return fail(e, ES_ERR_ARG, "long_split must be 0 or 1");
@@ -2013,7 +2019,7 @@ es_status es_set_schedule(es_engine *e, const es_schedule *s) {
 
 es_status es_autotune(es_engine *e, const es_window *w, size_t n, int repeats, es_schedule *chosen) {
   if (!e || !w || n == 0 || repeats < 1 || repeats > 1000) return ES_ERR_ARG;
-  static const uint32_t SHORT[] = {64, 128, 256};
+  static const uint32_t SHORT[] = {SEG_SMALL / 4, SEG_SMALL / 2, SEG_SMALL};
   static const uint32_t RUNG[] = {4, 6, 8};
   static const uint32_t SPLIT[] = {1, 0};
   const es_schedule before = e->sched;
@@ -2067,6 +2073,7 @@ es_status es_info(const es_engine *e, es_info_t *o) {
   o->cover_pmax = e->cover_pmax; o->floor = std::max(e->wheel_pmin, e->cover_pmax);
   o->ceiling = DIRECT_PMAX; o->class_fnv64 = e->class_fnv; o->filter_fnv64 = e->filter_fnv;
   o->n_certified = e->ncov; o->n_filters = e->mods.size(); o->mmax = e->mmax;
+  o->short_max_limit = es::SEG_SMALL;
   o->pinned = e->pin != nullptr;
   snprintf(o->classes_sha256, sizeof o->classes_sha256, "%s", e->pin ? e->pin->sha256 : "unpinned");
   return ES_OK;

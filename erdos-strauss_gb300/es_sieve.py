@@ -65,7 +65,8 @@ class Window(C.Structure):
 
 class Info(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("wheel_M", "lanes", "wheel_pmin", "cover_pmax", "floor", "ceiling",
-                                          "class_fnv64", "filter_fnv64", "n_certified", "n_filters", "mmax")] + \
+                                          "class_fnv64", "filter_fnv64", "n_certified", "n_filters", "mmax",
+                                          "short_max_limit")] + \
                [("pinned", C.c_int), ("classes_sha256", C.c_char * 72)]
 
 

@@ -111,6 +111,7 @@ typedef struct {
   uint64_t n_certified;     /* ncov */
   uint64_t n_filters;       /* certified + stage-B' primes */
   uint64_t mmax;
+  uint64_t short_max_limit; /* largest es_schedule.short_max (the kill-mask repeat, positions) */
   int pinned;               /* 1 if M has a pinned class-table digest */
   char classes_sha256[72];  /* the pin, or "unpinned" */
 } es_info_t;
@@ -185,9 +186,9 @@ size_t es_format_summary(const es_engine *engine, uint64_t lo, uint64_t hi, cons
  * records; only the time differs. No reference counterpart (the reference's CPU loop has
  * nothing to schedule). */
 typedef struct {
-  uint32_t short_max;            /* windows whose lanes hold at most this many positions (1..256)
-                                    are marked by the short-window kernel, longer ones by the
-                                    segment marking; default 256 */
+  uint32_t short_max;            /* windows whose lanes hold at most this many positions
+                                    (1..es_info_t.short_max_limit, 128 in this build) go to the
+                                    short-window kernel as they are; default the limit */
   uint32_t rung_blocks_per_sm;   /* stage-D grid in blocks per SM (1..16); default 6 */
   uint32_t long_split;           /* 1 (default): longer windows are cut into sub-windows of
                                     short_max positions per lane for the short-window kernel;
@@ -199,7 +200,7 @@ es_status es_get_schedule(const es_engine *engine, es_schedule *out);
 /* ES_ERR_ARG for a value out of range; captured batch graphs are rebuilt on the next run. */
 es_status es_set_schedule(es_engine *engine, const es_schedule *s);
 /* Autotuner: runs the windows (persistent schedule) under each candidate schedule -- short_max
- * in {64, 128, 256} x rung_blocks_per_sm in {4, 6, 8} x long_split in {1, 0} -- once to warm up
+ * in {limit/4, limit/2, limit} x rung_blocks_per_sm in {4, 6, 8} x long_split in {1, 0} -- once to warm up
  * and `repeats` times
  * timed, keeps the best device time of each, checks that every candidate gave identical
  * counters and records (ES_ERR_DEVICE_STATUS if not), and sets the fastest. `chosen` may be

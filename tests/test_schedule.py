@@ -23,6 +23,11 @@ def eng():
     e.close()
 
 
+def _smax(eng):
+    """The engine's largest short_max: its default schedule's (the kill-mask repeat)."""
+    return eng.info()["short_max_limit"]
+
+
 def _windows():
     wins = [tuple(int(x) for x in ln.split()) for ln in read("gen", "batch48.windows").splitlines()]
     g = workloads.SplitMix64(4242)
@@ -34,17 +39,18 @@ def _windows():
 
 def test_every_schedule_gives_identical_results(eng):
     wins = _windows()
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=0)
+    top = _smax(eng)
+    eng.set_schedule(short_max=top, rung_blocks_per_sm=6, long_split=0)
     base_c, base_r = eng.run_batch(wins)
     for split in (0, 1):
-        for sm in (1, 32, 64, 128, 200, 256):
+        for sm in sorted({1, 32, top // 2, top - 1, top}):
             for rb in (1, 4, 8, 16):
                 eng.set_schedule(short_max=sm, rung_blocks_per_sm=rb, long_split=split)
                 for sched in (es_sieve.ES_SCHED_PERSISTENT, es_sieve.ES_SCHED_PLAIN):
                     c, r = eng.run_batch(wins, schedule=sched)
                     assert c == base_c, (split, sm, rb, sched)
                     assert r.tobytes() == base_r.tobytes(), (split, sm, rb, sched)
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=1)
+    eng.set_schedule(short_max=top, rung_blocks_per_sm=6, long_split=1)
 
 
 def test_long_windows_split_or_segmented_agree(eng):
@@ -69,20 +75,22 @@ def test_autotune_picks_a_candidate_and_keeps_results(eng):
     wins = workloads.batch_windows(256, seed=77)
     before_c, before_r = eng.run_batch(wins)
     chosen = eng.autotune(wins, repeats=1)
-    assert chosen["short_max"] in (64, 128, 256) and chosen["rung_blocks_per_sm"] in (4, 6, 8)
+    top = _smax(eng)
+    assert chosen["short_max"] in (top // 4, top // 2, top) and chosen["rung_blocks_per_sm"] in (4, 6, 8)
     assert chosen["long_split"] in (0, 1)
     assert eng.schedule() == chosen
     c, r = eng.run_batch(wins)
     assert c == before_c and r.tobytes() == before_r.tobytes()
-    eng.set_schedule(short_max=256, rung_blocks_per_sm=6, long_split=1)
+    eng.set_schedule(short_max=top, rung_blocks_per_sm=6, long_split=1)
 
 
 def test_schedule_refusals(eng):
-    for kw in (dict(short_max=0), dict(short_max=257), dict(rung_blocks_per_sm=0), dict(rung_blocks_per_sm=17)):
+    top = _smax(eng)
+    for kw in (dict(short_max=0), dict(short_max=top + 1), dict(rung_blocks_per_sm=0), dict(rung_blocks_per_sm=17)):
         with pytest.raises(es_sieve.EsError) as ex:
             eng.set_schedule(**kw)
         assert ex.value.status == es_sieve.ES_ERR_ARG
-    assert eng.schedule() == {"short_max": 256, "rung_blocks_per_sm": 6, "long_split": 1}
+    assert eng.schedule() == {"short_max": top, "rung_blocks_per_sm": 6, "long_split": 1}
     with pytest.raises(es_sieve.EsError) as ex:
         eng.set_schedule(long_split=2)
     assert ex.value.status == es_sieve.ES_ERR_ARG
