@@ -40,10 +40,11 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
 METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch: one ncu
-# capture of this kernel on this workload (dram__bytes_read.sum 89.26 MB +
-# dram__bytes_write.sum 3.67 MB); scaled by the mask bytes when another batch size is run.
-MARK_SHORT_TRAFFIC_4096 = 89.263872e6 + 3.667968e6
-MARK_SHORT_INST_4096 = 873845259             # smsp__inst_executed.sum of the same capture
+# capture of this kernel on this workload (dram__bytes_read.sum 79.56 MB +
+# dram__bytes_write.sum 2.44 MB); scaled by the algorithmic bytes when another batch size is run.
+MARK_SHORT_TRAFFIC_4096 = 79.559680e6 + 2.436608e6
+MARK_SHORT_ALG_4096 = 79280448               # the same launch's algorithmic bytes
+MARK_SHORT_INST_4096 = 823032516             # smsp__inst_executed.sum of the same capture
 
 
 def parse():
@@ -410,7 +411,7 @@ def run_gpu(args, ws, rank, local):
     if dom == "k_mark_short":
         # one kill-mask row per lane from HBM, plus the per-window stride residues and window list
         alg = last_t["mask_bytes"] + len(wins) * 263 * 2 + len(wins) * 32
-        traffic = MARK_SHORT_TRAFFIC_4096 * alg / 88992512 if args.windows != 4096 else MARK_SHORT_TRAFFIC_4096
+        traffic = MARK_SHORT_TRAFFIC_4096 * alg / MARK_SHORT_ALG_4096 if args.windows != 4096 else MARK_SHORT_TRAFFIC_4096
     else:
         # the survivor tail: 24 B in and 64 B out per prime
         alg = int(last_t["primes"]) * (24 + 64)
