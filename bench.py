@@ -45,6 +45,9 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 MARK_SHORT_TRAFFIC_4096 = 79.559680e6 + 2.436608e6
 MARK_SHORT_ALG_4096 = 79280448               # the same launch's algorithmic bytes
 MARK_SHORT_INST_4096 = 823032516             # smsp__inst_executed.sum of the same capture
+# Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
+# position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
+MARKS_PER_INTEGER_GPU = 9.0951 / (2042040 / 2308)
 
 
 def parse():
@@ -429,6 +432,18 @@ def run_gpu(args, ws, rank, local):
         peak_issue = 152 * 4 * mhz * 1e6
         roof["issue"] = {"achieved": inst / (per_launch_ms / 1000.0), "peak": peak_issue, "unit": "warp inst/s",
                          "frac": inst / (per_launch_ms / 1000.0) / peak_issue, "inst_per_launch": inst}
+    if dom == "k_mark_short" and args.sieve == 0:
+        # The per-mark view: a segment sieve clears one bit per mark with a 4-byte shared-memory
+        # read-modify-write (8 bytes); the kill-mask kernel does no per-mark work, so this is the
+        # bandwidth such a sieve would need to match it, against the nominal shared-memory rate
+        # (152 SMs x 128 B per cycle at the sampled clock).
+        marks = n_int * MARKS_PER_INTEGER_GPU
+        mhz = clocks.get("sm_mhz") or 2070.0
+        smem_peak = 152 * 128 * mhz * 1e6 / 1e9
+        rmw_gbs = marks * 8 / (per_launch_ms / 1000.0) / 1e9
+        roof["marks"] = {"per_launch": marks, "achieved": marks / (per_launch_ms / 1000.0), "unit": "marks/s",
+                         "rmw_equivalent_gbs": rmw_gbs, "smem_peak_gbs": smem_peak, "peak_kind": "nominal",
+                         "frac": rmw_gbs / smem_peak}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
