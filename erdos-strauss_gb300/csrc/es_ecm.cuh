@@ -1,0 +1,208 @@
+// es_ecm.cuh -- Lenstra's elliptic-curve method, one curve per lane, for the hard cofactors of
+// stage D.
+//
+// A cofactor that reaches this point is an odd composite below 2^64 with every prime factor
+// above 2^16, not a square, and Brent's rho has already walked it for a few hundred steps per
+// lane without a collision: in practice a product of two primes of 24-31 bits. For those the
+// expected rho walk grows like the square root of the smaller prime (about 20 K steps, 40 K
+// Montgomery multiplies, for two 31-bit primes, over 32 walks in lockstep), while one ECM
+// curve with B1 = 85 and B2 = 4250 costs about 2.6 K multiplies and succeeds for a 31-bit
+// prime with probability ~0.1 (~0.3 for a 24-bit one), so 32 curves in a warp succeed
+// together with probability ~0.96 in a fixed ~2.6 K multiplies. The reference factors with
+// rho alone (sieve/rung_scan3.cpp:333-369); the factorization of a number is unique, so the
+// method that finds a divisor cannot change any certificate.
+//
+// Curves: Montgomery form B y^2 = x^3 + A x^2 + x with Suyama's parametrization (sigma ->
+// u = sigma^2 - 5, v = 4 sigma, starting point (u^3 : v^3), (A + 2)/4 = (v - u)^3 (3u + v) /
+// (16 u^3 v)), whose group orders are divisible by 12. x-only arithmetic in projective
+// coordinates (Montgomery 1987): doubling and differential addition. Stage 1 multiplies by
+// k = product of the largest powers of the primes p <= B1 that are <= B1, with the ladder;
+// stage 2 is the standard baby-step giant-step continuation with D = 60: for every prime q in
+// (B1, B2], written q = mD +- j with j coprime to 60, the product accumulates
+// X([mD]Q) Z([j]Q) - X([j]Q) Z([mD]Q), with the baby steps normalised to Z = 1.
+//
+// Everything here is exact modular arithmetic modulo n in Montgomery form; a divisor comes
+// only out of gcd(., n), so it always divides n. All lanes of a warp run the same sequence of
+// curve operations (k and the stage-2 table are the same for every lane), so the warp stays
+// converged apart from the short gcd and inverse loops. Every loop is bounded.
+#pragma once
+#include "es_arith.cuh"
+
+namespace es {
+
+constexpr u32 ECM_B1 = 85;
+constexpr u32 ECM_B2 = 4250;
+constexpr u32 ECM_D = 60;
+// k = lcm(1..85) = prod over primes p <= 85 of p^floor(log_p 85): 123 bits, little-endian words.
+constexpr int ECM_K_BITS = 123;
+__constant__ const u32 ECM_K[4] = {0x7f832ec0u, 0x0f71d9b7u, 0x6dd5f436u, 0x06136311u};
+// The baby steps: j < D/2 odd and coprime to D.
+constexpr int ECM_NJ = 8;
+__constant__ const u32 ECM_J[ECM_NJ] = {1, 7, 11, 13, 17, 19, 23, 29};
+// Giant steps m = 1 .. ECM_M1 (ECM_M1 = floor((B2 + D/2) / D)); bit i of ECM_PAIRS[m - 1] is set
+// when m*D + J[i] or m*D - J[i] is a prime in (B1, B2]. Every prime of (B1, B2] is covered.
+constexpr int ECM_M1 = 71;
+__constant__ const unsigned char ECM_PAIRS[ECM_M1] = {
+    0x80, 0xfe, 0xff, 0xdf, 0xfe, 0xef, 0xed, 0xff, 0xf3, 0xfb, 0xfb, 0xef, 0xf6, 0xfd, 0xfe, 0x7e,
+    0xef, 0xfe, 0x5c, 0xfb, 0xf5, 0xfb, 0xab, 0x3f, 0xff, 0xf7, 0x7f, 0xfc, 0x3b, 0x5d, 0xbf, 0xae,
+    0xfb, 0xcd, 0xbd, 0xf3, 0x7b, 0x9f, 0x97, 0xf7, 0x7b, 0xf5, 0xcd, 0x72, 0xff, 0xb6, 0xf9, 0xf3,
+    0xd9, 0xe5, 0xe7, 0x15, 0xdf, 0x7c, 0xeb, 0x9d, 0x8a, 0x7c, 0xff, 0xfa, 0xdd, 0xef, 0x7d, 0x7e,
+    0xf6, 0x9a, 0xbb, 0xef, 0xbf, 0xf5, 0xb0};
+
+__device__ __forceinline__ u64 submod(u64 a, u64 b, u64 n) {   // a, b < n
+  return a >= b ? a - b : a + (n - b);
+}
+
+// a^-1 mod n for odd n > 1 and gcd(a, n) = 1, 0 < a < n (binary extended Euclid: x1 a = u and
+// x2 a = v mod n throughout). Every pass of the outer loop halves u or v at least once, so it
+// ends within 128 passes; the bound only guards the invariant. Returns 0 if it is hit.
+__device__ inline u64 inv_mod(u64 a, u64 n) {
+  u64 u = a, v = n, x1 = 1, x2 = 0;
+  for (int guard = 0; guard < 256; ++guard) {
+    if (u == 1) return x1;
+    if (v == 1) return x2;
+    while (!(u & 1)) { u >>= 1; x1 = (x1 & 1) ? (x1 >> 1) + (n >> 1) + 1 : x1 >> 1; }
+    while (!(v & 1)) { v >>= 1; x2 = (x2 & 1) ? (x2 >> 1) + (n >> 1) + 1 : x2 >> 1; }
+    if (u >= v) { u -= v; x1 = submod(x1, x2, n); }
+    else { v -= u; x2 = submod(x2, x1, n); }
+    if (u == 0 || v == 0) return 0;                  // gcd(a, n) > 1: not invertible
+  }
+  return 0;
+}
+
+struct XZ { u64 x, z; };
+
+// [2]P; a24 = (A + 2)/4.
+__device__ __forceinline__ XZ ecm_dbl(XZ P, u64 a24, const Mont &M) {
+  const u64 s = addmod(P.x, P.z, M.n), d = submod(P.x, P.z, M.n);
+  const u64 t1 = mmul(s, s, M), t2 = mmul(d, d, M);
+  const u64 t3 = submod(t1, t2, M.n);                          // 4xz
+  return XZ{mmul(t1, t2, M), mmul(t3, addmod(t2, mmul(a24, t3, M), M.n), M)};
+}
+// P + Q given D = P - Q.
+__device__ __forceinline__ XZ ecm_add(XZ P, XZ Q, XZ D, const Mont &M) {
+  const u64 u = mmul(submod(P.x, P.z, M.n), addmod(Q.x, Q.z, M.n), M);
+  const u64 v = mmul(addmod(P.x, P.z, M.n), submod(Q.x, Q.z, M.n), M);
+  const u64 s = addmod(u, v, M.n), d = submod(u, v, M.n);
+  return XZ{mmul(D.z, mmul(s, s, M), M), mmul(D.x, mmul(d, d, M), M)};
+}
+// P + Q given P - Q = (dx : 1).
+__device__ __forceinline__ XZ ecm_add1(XZ P, XZ Q, u64 dx, const Mont &M) {
+  const u64 u = mmul(submod(P.x, P.z, M.n), addmod(Q.x, Q.z, M.n), M);
+  const u64 v = mmul(addmod(P.x, P.z, M.n), submod(Q.x, Q.z, M.n), M);
+  const u64 s = addmod(u, v, M.n), d = submod(u, v, M.n);
+  return XZ{mmul(s, s, M), mmul(dx, mmul(d, d, M), M)};
+}
+
+// Montgomery form of w^-1 for a Montgomery residue w (w = W 2^64 mod n): 0 if not invertible.
+__device__ __forceinline__ u64 mont_inverse(u64 w, const Mont &M) {
+  const u64 t = inv_mod(w, M.n);                               // W^-1 2^-64
+  if (!t) return 0;
+  return mmul(mmul(t, M.r2, M), M.r2, M);                      // W^-1, then W^-1 2^64
+}
+
+// Divisor d of n from gcd(g, n), if it is a proper one; else 0.
+__device__ __forceinline__ u64 proper_gcd(u64 g, u64 n) {
+  const u64 d = gcd64(g, n);
+  return (d > 1 && d < n) ? d : 0;
+}
+
+// Stage-2 steps charged per ECM_STAGE2_POLL giant steps between polls.
+constexpr int ECM_STAGE2_POLL = 24;
+
+// One ECM curve (Suyama's sigma, 6 <= sigma < n) on the odd composite n > 2^32. Returns a
+// proper divisor of n, or 0 when this curve found none. poll() is called at the same points
+// in every lane (after stage 1 and every ECM_STAGE2_POLL giant steps); when it returns true
+// the curve stops early and returns 0. dead lanes keep computing (their result is dropped)
+// so that the lanes of a warp stay in step.
+template <class Poll>
+__device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
+  const u64 n = M.n;
+  u64 found = 0;
+  bool dead = false;
+  // --- the curve and its starting point
+  const u64 sm = to_mont(sigma, M);
+  const u64 five = to_mont(5, M);
+  const u64 u = submod(mmul(sm, sm, M), five, n);
+  const u64 v2 = addmod(sm, sm, n), v = addmod(v2, v2, n);
+  const u64 u3 = mmul(mmul(u, u, M), u, M), v3 = mmul(mmul(v, v, M), v, M);
+  const u64 vu = submod(v, u, n);
+  const u64 num = mmul(mmul(mmul(vu, vu, M), vu, M), addmod(addmod(addmod(u, u, n), u, n), v, n), M);
+  u64 den = mmul(u3, v, M);
+  #pragma unroll
+  for (int i = 0; i < 4; ++i) den = addmod(den, den, n);      // 16 u^3 v
+  const u64 w = mmul(den, v3, M);
+  u64 winv = 0;
+  {
+    const u64 g = gcd64(w, n);
+    if (g != 1) { dead = true; if (g < n) found = g; }
+    else winv = mont_inverse(w, M);
+    if (!winv) dead = true;
+  }
+  const u64 x = mmul(mmul(u3, den, M), winv, M);               // u^3 / v^3
+  const u64 a24 = mmul(mmul(num, v3, M), winv, M);             // (A + 2) / 4
+  // --- stage 1: Q = [k](x : 1), ladder from the top bit of k
+  XZ R0{x, M.one}, R1 = ecm_dbl(R0, a24, M);
+  for (int i = ECM_K_BITS - 2; i >= 0; --i) {
+    const bool b = (ECM_K[i >> 5] >> (i & 31)) & 1u;
+    if (b) { const XZ t = R0; R0 = R1; R1 = t; }
+    R1 = ecm_add1(R0, R1, x, M);
+    R0 = ecm_dbl(R0, a24, M);
+    if (b) { const XZ t = R0; R0 = R1; R1 = t; }
+  }
+  const XZ Q = R0;
+  if (!dead) {
+    const u64 g = gcd64(Q.z, n);
+    if (g != 1) { dead = true; if (g < n) found = g; }
+  }
+  if (poll()) return 0;
+  // --- stage 2: baby steps [j]Q for odd j <= 31 (kept for j in ECM_J), giant step [60]Q
+  const XZ Q2 = ecm_dbl(Q, a24, M);
+  u64 bx[ECM_NJ], bz[ECM_NJ];
+  bx[0] = Q.x; bz[0] = Q.z;
+  XZ prev = Q, cur = ecm_add(Q2, Q, Q, M);                     // [1], [3]
+  int nb = 1;
+  XZ P29{0, 0};
+  #pragma unroll
+  for (int j = 3; j <= 29; j += 2) {                           // cur = [j]
+    if (j % 3 != 0 && j % 5 != 0) { bx[nb] = cur.x; bz[nb] = cur.z; ++nb; }
+    if (j == 29) P29 = cur;
+    const XZ nxt = ecm_add(cur, Q2, prev, M);                  // [j + 2]
+    prev = cur; cur = nxt;
+  }
+  const XZ G1 = ecm_add(cur, P29, Q2, M);                      // [31] + [29] = [60]
+  // normalise the baby steps: xn[i] = X_j / Z_j (one inverse for all eight)
+  u64 c[ECM_NJ];
+  c[0] = bz[0];
+  #pragma unroll
+  for (int i = 1; i < ECM_NJ; ++i) c[i] = mmul(c[i - 1], bz[i], M);
+  u64 inv = 0;
+  if (!dead) {
+    const u64 g = gcd64(c[ECM_NJ - 1], n);
+    if (g != 1) { dead = true; if (g < n) found = g; }
+    else { inv = mont_inverse(c[ECM_NJ - 1], M); if (!inv) dead = true; }
+  }
+  u64 xn[ECM_NJ];
+  #pragma unroll
+  for (int i = ECM_NJ - 1; i > 0; --i) {
+    xn[i] = mmul(bx[i], mmul(inv, c[i - 1], M), M);
+    inv = mmul(inv, bz[i], M);
+  }
+  xn[0] = mmul(bx[0], inv, M);
+  // giant steps G_m = [60 m]Q, m = 1 .. ECM_M1
+  u64 acc = M.one;
+  XZ Gp = G1, G = G1;
+  for (int m = 1; m <= ECM_M1; ++m) {
+    if (m == 2) G = ecm_dbl(G1, a24, M);
+    else if (m > 2) { const XZ t = ecm_add(G, G1, Gp, M); Gp = G; G = t; }
+    const u32 mask = ECM_PAIRS[m - 1];
+    #pragma unroll
+    for (int i = 0; i < ECM_NJ; ++i)
+      if (mask & (1u << i)) acc = mmul(acc, submod(G.x, mmul(xn[i], G.z, M), n), M);
+    if (m % ECM_STAGE2_POLL == 0 && poll()) return 0;
+  }
+  if (!dead) found = proper_gcd(acc, n);
+  return found;
+}
+
+}  // namespace es

@@ -637,6 +637,9 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
 #define ES_RUNG_WARPS 4
 #endif
 constexpr int RUNG_WARPS = ES_RUNG_WARPS;
+#ifndef ES_RUNG_MIN_BLOCKS
+#define ES_RUNG_MIN_BLOCKS (16 / RUNG_WARPS)   // resident blocks per SM the register budget allows
+#endif
 #ifndef ES_HELP_BLOCKS_PER_SM
 #define ES_HELP_BLOCKS_PER_SM 1
 #endif
@@ -667,7 +670,7 @@ __device__ __forceinline__ void rung_result(const TailParams &T, const Surv &s, 
   atomicAdd(T.rung_done, 1ull);
 }
 
-__global__ void __launch_bounds__(RUNG_WARPS * 32, 16 / RUNG_WARPS) k_rung(const TailParams T, int no_rung) {
+__global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(const TailParams T, int no_rung) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -753,7 +756,7 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
     if (lane == 0) out[i] = pr ? 1 : 0;
   }
 }
-__global__ void __launch_bounds__(RUNG_WARPS * 32, 16 / RUNG_WARPS) k_probe_rung(const u64 *p, u64 count, RecDev *out,
+__global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
                                                                const TdEntry *tde, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[RUNG_WARPS];

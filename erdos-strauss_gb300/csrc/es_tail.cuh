@@ -9,12 +9,15 @@
 //   primality        lanes 0..11 each run one of the 12 strong-probable-prime rounds
 //   Brent's rho      all 32 lanes walk with different constants c; the first split wins
 //                    (the factorization is unique, so which lane wins cannot change it)
+//   ECM              a cofactor rho has not split after ECM_AFTER steps gets one elliptic
+//                    curve per lane (es_ecm.cuh), the first divisor wins
 //   rung DP          lanes own residue classes t mod r and gather
 //                    nxt[t] = min_j cur[t * pr^-j] * pr^j over j <= e with the bound <= q
 // and a block of four warps walks successive rungs of one prime concurrently, keeping the
 // smallest rung that certifies (the reference's emission rule, sieve/rung_scan3.cpp:574-603).
 #pragma once
 #include "es_arith.cuh"
+#include "es_ecm.cuh"
 
 namespace es {
 
@@ -105,12 +108,15 @@ __device__ __forceinline__ bool cancelled(const volatile int *cancel, int my_k) 
   return cancel && *cancel < my_k;
 }
 
-// The hard board: a cofactor whose rho is still running after RHO_POST_STEPS steps is posted
-// here, and warps with nothing left to do (k_rung blocks that found the prime queue empty) run
-// more walks on it with constants of their own. Any nontrivial divisor ends the search; by the
-// birthday bound the wait for the first collision among W walks shrinks like 1/sqrt(W). The
-// board only speeds things up: the owner checks every divisor it is handed (1 < d < n,
-// n mod d == 0) and its own walks still finish the job alone. No warp ever waits for another.
+// The hard board: a cofactor that rho has not split in its first steps is posted here when its
+// owner turns to ECM, and warps with nothing left to do (k_rung blocks that found the prime
+// queue empty) run more rho walks on it with constants of their own. Any nontrivial divisor
+// ends the search; by the birthday bound the wait for the first collision among W walks
+// shrinks like 1/sqrt(W), so with hundreds of idle warps the helpers' walks can beat the
+// owner's fixed-length ECM round, while a cofactor left alone gets the ECM round. The board
+// only speeds things up: the owner checks every divisor it is handed (1 < d < n,
+// n mod d == 0) and its own curves and walks still finish the job alone. No warp ever waits
+// for another.
 constexpr u32 HARD_SLOTS = 32;                 // one per lane of a scanning warp
 #ifndef ES_RHO_POST_STEPS
 #define ES_RHO_POST_STEPS 512
@@ -186,10 +192,38 @@ __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep,
   }
 }
 
+// One round of ECM_CURVES-per-warp elliptic curves on n: lane l takes sigma0 + l. poll()
+// returns what rho_walk's does (a divisor handed in, ~0 to stop, 0 to go on); a nonzero answer
+// ends the round and is left in ext. Returns the first divisor a lane found (the same value in
+// every lane), or 0.
+template <class Poll>
+__device__ inline u64 warp_ecm(const Mont &M, u64 sigma0, u32 lane, Poll poll, u64 &ext) {
+  ext = 0;
+  auto p = [&]() -> bool { ext = poll(); return ext != 0; };
+  const u64 d = ecm_curve(sigma0 + lane, M, p);
+  const unsigned has = __ballot_sync(FULL, d != 0);
+  return has ? __shfl_sync(FULL, d, __ffs(has) - 1) : 0;
+}
+
+// Rho steps per lane before a cofactor goes to ECM: rho is the cheaper method for a prime
+// factor below ~2^22 (its expected walk over 32 lanes is a few hundred steps), ECM above.
+#ifndef ES_ECM_AFTER
+#define ES_ECM_AFTER 512
+#endif
+constexpr u64 ECM_AFTER = ES_ECM_AFTER;
+constexpr u64 ECM_ROUND_STEPS = 1400;    // one round (~2.7 K multiplies) in rho steps of 2 multiplies
+constexpr u32 ECM_OWNER_ROUNDS = 16;     // 512 curves: a 31-bit factor survives them w.p. < 1e-20
+constexpr u64 ECM_SIGMA_OWNER = 6;       // owner round r: sigma = 6 + 32 r + lane
+constexpr u64 ECM_SIGMA_HELP = 1024;     // helper session s (ES_HELP_ECM): 1024 + 32 (s mod 2^20) + lane
+#ifndef ES_HELP_ECM
+#define ES_HELP_ECM 0                    // helpers run ECM rounds (1) or rho walks (0)
+#endif
+
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
                                int my_k = 0, const HardBoard *board = nullptr, u64 budget = WARP_RHO_STEPS) {
   const Mont M = mont_init(n);
   int slot = -1;                                   // the board slot this warp posted n in
+  bool stop = false;                               // cancelled (warp-uniform)
   auto poll = [&](u64 steps) -> u64 {
     u64 ext = 0;
     if (lane == 0) {
@@ -210,9 +244,26 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
         if (d > 1 && d < n && n % d == 0) ext = d;
       }
     }
-    return __shfl_sync(FULL, ext, 0);
+    ext = __shfl_sync(FULL, ext, 0);
+    if (ext == ~0ull) stop = true;
+    return ext;
   };
-  const u64 f = rho_walk(n, M, 1 + lane, 32, budget, lane, poll);
+  // Brent's rho first; a cofactor it has not split goes to ECM rounds (charged against the same
+  // budget), and rho resumes with fresh constants for whatever budget remains after them.
+  const bool ecm = budget >= ECM_AFTER + ECM_ROUND_STEPS;
+  u64 f = rho_walk(n, M, 1 + lane, 32, ecm ? ECM_AFTER : budget, lane, poll);
+  if (!f && !stop && ecm) {
+    u64 steps = ECM_AFTER;
+    u64 ext = poll(RHO_POST_STEPS > steps ? RHO_POST_STEPS : steps);   // post n to the board now
+    if (ext && ext != ~0ull) f = ext;
+    for (u32 round = 0; !f && !stop && round < ECM_OWNER_ROUNDS && steps + ECM_ROUND_STEPS <= budget; ++round) {
+      f = warp_ecm(M, ECM_SIGMA_OWNER + 32 * (u64)round, lane, [&]() -> u64 { return poll(steps); }, ext);
+      steps += ECM_ROUND_STEPS;
+      if (!f && ext && ext != ~0ull) f = ext;
+    }
+    if (!f && !stop && steps < budget)
+      f = rho_walk(n, M, 1 + lane + 32 * 1024, 32, budget - steps, lane, poll);
+  }
   if (lane == 0 && slot >= 0 && slot < (int)HARD_SLOTS) {  // take n off the board
     atomicExch(&board->slot[slot].state, 1u);
     board->slot[slot].n = 0;
@@ -228,9 +279,8 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
 
 // A warp with nothing left to do helps the posted cofactors until every prime of the run is
 // finished (or the board stays empty for HELP_IDLE_POLLS polls, or after HELP_MAX_ROUNDS
-// sessions): each session picks a posted
-// slot, walks HELP_STEPS steps per lane with constants no other walk uses, and posts the
-// first divisor it finds. All lanes call.
+// sessions): each session picks a posted slot, walks HELP_STEPS steps per lane with constants
+// no other walk uses, and posts the first divisor it finds. All lanes call.
 __device__ inline void warp_help(const HardBoard &B, u32 lane) {
   for (u32 idle = 0, round = 0; idle < HELP_IDLE_POLLS && round < HELP_MAX_ROUNDS + HELP_IDLE_POLLS; ++round) {
     if (ld_volatile(B.done) >= B.total) return;
@@ -253,18 +303,22 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
     __threadfence();
     if (ld_volatile(&hs->state) != 2u || n <= 0xFFFFFFFFull || !(n & 1)) continue;
     const Mont M = mont_init(n);
-    // constants above every owner's (an owner walks c = 1 + lane + 32 j with j far below 2^19),
-    // distinct per session (2^20 sessions apart before a restart adds 2^25)
-    const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
     auto poll = [&](u64) -> u64 {
       u64 ext = 0;
       if (lane == 0)
         ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
       return __shfl_sync(FULL, ext, 0);
     };
-    // a posted cofactor has already outlasted RHO_POST_STEPS of its owner's walks: helpers
-    // start with a longer comparison window
+#if ES_HELP_ECM
+    u64 ext = 0;
+    const u64 d = warp_ecm(M, ECM_SIGMA_HELP + 32 * (ses & 0xFFFFFull), lane, [&]() -> u64 { return poll(0); }, ext);
+#else
+    // constants above every owner's (an owner walks c = 1 + lane + 32 j with j below 2^12),
+    // distinct per session (2^20 sessions apart before a restart adds 2^25); a posted cofactor
+    // has already outlasted its owner's first walks, so helpers start with a longer window
+    const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
     const u64 d = rho_walk(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
+#endif
     if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
       atomicCAS(&hs->found, 0ull, (unsigned long long)d);
     __syncwarp();

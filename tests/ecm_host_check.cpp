@@ -1,0 +1,78 @@
+// Host build of the device ECM (erdos-strauss_gb300/csrc/es_ecm.cuh) for the CPU tests: the
+// same source compiled by g++ with the four device intrinsics it uses defined on 128-bit host
+// integers. Checks the binary inverse on random residues, then runs 32 curves (sigma 6..37,
+// one warp's first round) on seeded semiprimes with prime factors of 18-31 bits and prints the
+// fraction of curves that split each size; every divisor returned must divide n properly.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#define __device__
+#define __forceinline__ inline
+#define __constant__
+static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+}
+static inline int __ffsll(long long x) { return x ? __builtin_ctzll((unsigned long long)x) + 1 : 0; }
+static inline unsigned atomicOr(unsigned *p, unsigned v) { const unsigned o = *p; *p |= v; return o; }
+#include "es_ecm.cuh"
+using namespace es;
+
+static const u64 BASES[12] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+static bool is_prime(u64 n) {
+  if (n < 2) return false;
+  for (u64 b : BASES) if (n % b == 0) return n == b;
+  u64 d = n - 1;
+  int s = 0;
+  while (!(d & 1)) { d >>= 1; ++s; }
+  for (u64 a : BASES) {
+    unsigned __int128 x = 1, b = a;
+    for (u64 e = d; e; e >>= 1) { if (e & 1) x = x * b % n; b = b * b % n; }
+    if (x == 1 || x == n - 1) continue;
+    bool ok = false;
+    for (int i = 1; i < s && !ok; ++i) { x = x * x % n; ok = x == n - 1; }
+    if (!ok) return false;
+  }
+  return true;
+}
+static u64 random_prime(int bits, std::mt19937_64 &g) {
+  for (;;) {
+    const u64 p = (g() & ((1ull << bits) - 1)) | (1ull << (bits - 1)) | 1;
+    if (is_prime(p)) return p;
+  }
+}
+
+int main(int argc, char **argv) {
+  const int trials = argc > 1 ? atoi(argv[1]) : 40;
+  std::mt19937_64 g(0xE52026);
+  for (int t = 0; t < 20000; ++t) {
+    const u64 n = g() | 1, a = g() % n;
+    if (n < 3 || !a) continue;
+    const u64 x = inv_mod(a, n);
+    if (gcd64(a, n) == 1 ? (unsigned __int128)a * x % n != 1 : x != 0) {
+      printf("FAIL inverse a=%llu n=%llu\n", a, n);
+      return 1;
+    }
+  }
+  for (int bits = 18; bits <= 31; ++bits) {
+    int split = 0, curves = 0, warps = 0;
+    for (int t = 0; t < trials; ++t) {
+      const u64 p = random_prime(bits, g), q = random_prime(62 - bits, g), n = p * q;
+      const Mont M = mont_init(n);
+      bool any = false;
+      for (u64 lane = 0; lane < 32; ++lane, ++curves) {
+        const u64 d = ecm_curve(6 + lane, M, [] { return false; });
+        if (!d) continue;
+        if (d <= 1 || d >= n || n % d) {
+          printf("FAIL divisor %llu of %llu\n", d, n);
+          return 1;
+        }
+        ++split;
+        any = true;
+      }
+      warps += any;
+    }
+    printf("bits %d curves %.3f warps %.3f\n", bits, (double)split / curves, (double)warps / trials);
+  }
+  return 0;
+}
