@@ -6,11 +6,15 @@
 // lane without a collision: in practice a product of two primes of 24-31 bits. For those the
 // expected rho walk grows like the square root of the smaller prime (about 20 K steps, 40 K
 // Montgomery multiplies, for two 31-bit primes, over 32 walks in lockstep), while one ECM
-// curve with B1 = 85 and B2 = 4250 costs about 2.6 K multiplies and succeeds for a 31-bit
-// prime with probability ~0.1 (~0.3 for a 24-bit one), so 32 curves in a warp succeed
-// together with probability ~0.96 in a fixed ~2.6 K multiplies. The reference factors with
-// rho alone (sieve/rung_scan3.cpp:333-369); the factorization of a number is unique, so the
-// method that finds a divisor cannot change any certificate.
+// curve with B1 = 40 and B2 = 2000 costs about 1.3 K multiplies and succeeds with probability
+// ~0.02 for a 31-bit prime, ~0.15 for a 24-bit one: a round of 32 curves in a warp splits a
+// 31-bit pair about half the time, a 24-bit one almost always. On GB300 a single warp's
+// multiply chain is latency-bound (about 0.1 us per 64-bit Montgomery multiply), so short
+// rounds that fail now and then beat long sure ones: measured on the 4096-window batch, stage D
+// took 0.45 ms with B1 = 40, 0.47 with 50, 0.48 with 60, 0.55 with 85 and 0.49 with 30, whose
+// 2^34 window at 1.8e19 then needed 2.1 ms (too many failed rounds). The reference factors
+// with rho alone (sieve/rung_scan3.cpp:333-369); the factorization of a number is unique, so
+// the method that finds a divisor cannot change any certificate.
 //
 // Curves: Montgomery form B y^2 = x^3 + A x^2 + x with Suyama's parametrization (sigma ->
 // u = sigma^2 - 5, v = 4 sigma, starting point (u^3 : v^3), (A + 2)/4 = (v - u)^3 (3u + v) /
@@ -30,24 +34,25 @@
 
 namespace es {
 
-constexpr u32 ECM_B1 = 85;
-constexpr u32 ECM_B2 = 4250;
+constexpr u32 ECM_B1 = 40;
+constexpr u32 ECM_B2 = 2000;
 constexpr u32 ECM_D = 60;
-// k = lcm(1..85) = prod over primes p <= 85 of p^floor(log_p 85): 123 bits, little-endian words.
-constexpr int ECM_K_BITS = 123;
-__constant__ const u32 ECM_K[4] = {0x7f832ec0u, 0x0f71d9b7u, 0x6dd5f436u, 0x06136311u};
+// k = lcm(1..40) = prod over primes p <= 40 of p^floor(log_p 40): 53 bits, little-endian words.
+constexpr int ECM_K_BITS = 53;
+__constant__ const u32 ECM_K[2] = {0x2b8eb920u, 0x0012fb5eu};
 // The baby steps: j < D/2 odd and coprime to D.
 constexpr int ECM_NJ = 8;
 __constant__ const u32 ECM_J[ECM_NJ] = {1, 7, 11, 13, 17, 19, 23, 29};
 // Giant steps m = 1 .. ECM_M1 (ECM_M1 = floor((B2 + D/2) / D)); bit i of ECM_PAIRS[m - 1] is set
 // when m*D + J[i] or m*D - J[i] is a prime in (B1, B2]. Every prime of (B1, B2] is covered.
-constexpr int ECM_M1 = 71;
+constexpr int ECM_M1 = 33;
 __constant__ const unsigned char ECM_PAIRS[ECM_M1] = {
-    0x80, 0xfe, 0xff, 0xdf, 0xfe, 0xef, 0xed, 0xff, 0xf3, 0xfb, 0xfb, 0xef, 0xf6, 0xfd, 0xfe, 0x7e,
+    0xff, 0xfe, 0xff, 0xdf, 0xfe, 0xef, 0xed, 0xff, 0xf3, 0xfb, 0xfb, 0xef, 0xf6, 0xfd, 0xfe, 0x7e,
     0xef, 0xfe, 0x5c, 0xfb, 0xf5, 0xfb, 0xab, 0x3f, 0xff, 0xf7, 0x7f, 0xfc, 0x3b, 0x5d, 0xbf, 0xae,
-    0xfb, 0xcd, 0xbd, 0xf3, 0x7b, 0x9f, 0x97, 0xf7, 0x7b, 0xf5, 0xcd, 0x72, 0xff, 0xb6, 0xf9, 0xf3,
-    0xd9, 0xe5, 0xe7, 0x15, 0xdf, 0x7c, 0xeb, 0x9d, 0x8a, 0x7c, 0xff, 0xfa, 0xdd, 0xef, 0x7d, 0x7e,
-    0xf6, 0x9a, 0xbb, 0xef, 0xbf, 0xf5, 0xb0};
+    0xbb};
+// One round (about 1.3 K Montgomery multiplies: 10 per bit of k, 2 per stage-2 pair, 6 per
+// giant step) in rho steps of two multiplies.
+constexpr u64 ECM_ROUND_STEPS = 700;
 
 __device__ __forceinline__ u64 submod(u64 a, u64 b, u64 n) {   // a, b < n
   return a >= b ? a - b : a + (n - b);

@@ -70,7 +70,9 @@ def test_host_build_splits_hard_semiprimes(tmp_path):
     rates = {int(m.group(1)): (float(m.group(2)), float(m.group(3)))
              for m in re.finditer(r"bits (\d+) curves ([\d.]+) warps ([\d.]+)", out.stdout)}
     assert sorted(rates) == list(range(18, 32))
-    # one round of 32 curves splits nearly every semiprime; the per-curve rate falls with the
-    # size of the smaller prime (about 0.8 at 18 bits, 0.1 at 31)
-    assert all(w >= 0.9 for _, w in rates.values()), rates
-    assert rates[18][0] > 0.6 and 0.04 < rates[31][0] < 0.25, rates
+    # the per-curve rate falls with the size of the smaller prime (B1 = 40, B2 = 2000: about
+    # 0.65 at 18 bits, 0.15 at 24, 0.02 at 31); one round of 32 curves splits every pair with
+    # a prime below 2^22 and about half of the 31-bit pairs
+    assert all(rates[b][1] == 1.0 for b in range(18, 23)), rates
+    assert rates[18][0] > 0.5 and 0.08 < rates[24][0] < 0.25 and 0.003 < rates[31][0] < 0.05, rates
+    assert rates[31][1] > 0.1, rates
