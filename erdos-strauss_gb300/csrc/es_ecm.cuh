@@ -25,8 +25,8 @@
 // (B1, B2], written q = mD +- j with j coprime to 60, the product accumulates
 // X([mD]Q) Z([j]Q) - X([j]Q) Z([mD]Q), with the baby steps normalised to Z = 1.
 //
-// Everything here is exact modular arithmetic modulo n in Montgomery form; a divisor comes
-// only out of gcd(., n), so it always divides n. All lanes of a warp run the same sequence of
+// Everything here is modular arithmetic modulo n in Montgomery form (the lazy representation of
+// es_arith.cuh for n < 2^62); a divisor comes only out of gcd(., n), so it always divides n. All lanes of a warp run the same sequence of
 // curve operations (k and the stage-2 table are the same for every lane), so the warp stays
 // converged apart from the short gcd and inverse loops. Every loop is bounded.
 #pragma once
@@ -77,33 +77,39 @@ __device__ inline u64 inv_mod(u64 a, u64 n) {
 
 struct XZ { u64 x, z; };
 
+// The curve operations over an arithmetic policy Ar (ExactArith or LazyArith, es_arith.cuh).
 // [2]P; a24 = (A + 2)/4.
+template <class Ar>
 __device__ __forceinline__ XZ ecm_dbl(XZ P, u64 a24, const Mont &M) {
-  const u64 s = addmod(P.x, P.z, M.n), d = submod(P.x, P.z, M.n);
-  const u64 t1 = mmul(s, s, M), t2 = mmul(d, d, M);
-  const u64 t3 = submod(t1, t2, M.n);                          // 4xz
-  return XZ{mmul(t1, t2, M), mmul(t3, addmod(t2, mmul(a24, t3, M), M.n), M)};
+  const u64 s = Ar::add(P.x, P.z, M), d = Ar::sub(P.x, P.z, M);
+  const u64 t1 = Ar::mul(s, s, M), t2 = Ar::mul(d, d, M);
+  const u64 t3 = Ar::sub(t1, t2, M);                           // 4xz
+  return XZ{Ar::mul(t1, t2, M), Ar::mul(t3, Ar::add(t2, Ar::mul(a24, t3, M), M), M)};
 }
 // P + Q given D = P - Q.
+template <class Ar>
 __device__ __forceinline__ XZ ecm_add(XZ P, XZ Q, XZ D, const Mont &M) {
-  const u64 u = mmul(submod(P.x, P.z, M.n), addmod(Q.x, Q.z, M.n), M);
-  const u64 v = mmul(addmod(P.x, P.z, M.n), submod(Q.x, Q.z, M.n), M);
-  const u64 s = addmod(u, v, M.n), d = submod(u, v, M.n);
-  return XZ{mmul(D.z, mmul(s, s, M), M), mmul(D.x, mmul(d, d, M), M)};
+  const u64 u = Ar::mul(Ar::sub(P.x, P.z, M), Ar::add(Q.x, Q.z, M), M);
+  const u64 v = Ar::mul(Ar::add(P.x, P.z, M), Ar::sub(Q.x, Q.z, M), M);
+  const u64 s = Ar::add(u, v, M), d = Ar::sub(u, v, M);
+  return XZ{Ar::mul(D.z, Ar::mul(s, s, M), M), Ar::mul(D.x, Ar::mul(d, d, M), M)};
 }
 // P + Q given P - Q = (dx : 1).
+template <class Ar>
 __device__ __forceinline__ XZ ecm_add1(XZ P, XZ Q, u64 dx, const Mont &M) {
-  const u64 u = mmul(submod(P.x, P.z, M.n), addmod(Q.x, Q.z, M.n), M);
-  const u64 v = mmul(addmod(P.x, P.z, M.n), submod(Q.x, Q.z, M.n), M);
-  const u64 s = addmod(u, v, M.n), d = submod(u, v, M.n);
-  return XZ{mmul(s, s, M), mmul(dx, mmul(d, d, M), M)};
+  const u64 u = Ar::mul(Ar::sub(P.x, P.z, M), Ar::add(Q.x, Q.z, M), M);
+  const u64 v = Ar::mul(Ar::add(P.x, P.z, M), Ar::sub(Q.x, Q.z, M), M);
+  const u64 s = Ar::add(u, v, M), d = Ar::sub(u, v, M);
+  return XZ{Ar::mul(s, s, M), Ar::mul(dx, Ar::mul(d, d, M), M)};
 }
 
-// Montgomery form of w^-1 for a Montgomery residue w (w = W 2^64 mod n): 0 if not invertible.
+// Montgomery form of w^-1 for a Montgomery residue w (w = W 2^64 mod n, any representative):
+// 0 if not invertible.
+template <class Ar>
 __device__ __forceinline__ u64 mont_inverse(u64 w, const Mont &M) {
-  const u64 t = inv_mod(w, M.n);                               // W^-1 2^-64
+  const u64 t = inv_mod(Ar::norm(w, M), M.n);                  // W^-1 2^-64
   if (!t) return 0;
-  return mmul(mmul(t, M.r2, M), M.r2, M);                      // W^-1, then W^-1 2^64
+  return Ar::mul(Ar::mul(t, M.r2, M), M.r2, M);                // W^-1, then W^-1 2^64
 }
 
 // Divisor d of n from gcd(g, n), if it is a proper one; else 0.
@@ -112,15 +118,15 @@ __device__ __forceinline__ u64 proper_gcd(u64 g, u64 n) {
   return (d > 1 && d < n) ? d : 0;
 }
 
-// Stage-2 steps charged per ECM_STAGE2_POLL giant steps between polls.
+// Giant steps between polls in stage 2.
 constexpr int ECM_STAGE2_POLL = 24;
 
-// One ECM curve (Suyama's sigma, 6 <= sigma < n) on the odd composite n > 2^32. Returns a
-// proper divisor of n, or 0 when this curve found none. poll() is called at the same points
-// in every lane (after stage 1 and every ECM_STAGE2_POLL giant steps); when it returns true
-// the curve stops early and returns 0. dead lanes keep computing (their result is dropped)
-// so that the lanes of a warp stay in step.
-template <class Poll>
+// One ECM curve (Suyama's sigma, 6 <= sigma < n) on the odd composite n > 2^32, in the
+// arithmetic Ar (LazyArith needs n < 2^62). Returns a proper divisor of n, or 0 when this curve
+// found none. poll() is called at the same points in every lane (after stage 1 and every
+// ECM_STAGE2_POLL giant steps); when it returns true the curve stops early and returns 0. dead
+// lanes keep computing (their result is dropped) so that the lanes of a warp stay in step.
+template <class Ar, class Poll>
 __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
   const u64 n = M.n;
   u64 found = 0;
@@ -128,31 +134,31 @@ __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
   // --- the curve and its starting point
   const u64 sm = to_mont(sigma, M);
   const u64 five = to_mont(5, M);
-  const u64 u = submod(mmul(sm, sm, M), five, n);
-  const u64 v2 = addmod(sm, sm, n), v = addmod(v2, v2, n);
-  const u64 u3 = mmul(mmul(u, u, M), u, M), v3 = mmul(mmul(v, v, M), v, M);
-  const u64 vu = submod(v, u, n);
-  const u64 num = mmul(mmul(mmul(vu, vu, M), vu, M), addmod(addmod(addmod(u, u, n), u, n), v, n), M);
-  u64 den = mmul(u3, v, M);
+  const u64 u = Ar::sub(Ar::mul(sm, sm, M), five, M);
+  const u64 v2 = Ar::add(sm, sm, M), v = Ar::add(v2, v2, M);
+  const u64 u3 = Ar::mul(Ar::mul(u, u, M), u, M), v3 = Ar::mul(Ar::mul(v, v, M), v, M);
+  const u64 vu = Ar::sub(v, u, M);
+  const u64 num = Ar::mul(Ar::mul(Ar::mul(vu, vu, M), vu, M), Ar::add(Ar::add(Ar::add(u, u, M), u, M), v, M), M);
+  u64 den = Ar::mul(u3, v, M);
   #pragma unroll
-  for (int i = 0; i < 4; ++i) den = addmod(den, den, n);      // 16 u^3 v
-  const u64 w = mmul(den, v3, M);
+  for (int i = 0; i < 4; ++i) den = Ar::add(den, den, M);      // 16 u^3 v
+  const u64 w = Ar::mul(den, v3, M);
   u64 winv = 0;
   {
     const u64 g = gcd64(w, n);
     if (g != 1) { dead = true; if (g < n) found = g; }
-    else winv = mont_inverse(w, M);
+    else winv = mont_inverse<Ar>(w, M);
     if (!winv) dead = true;
   }
-  const u64 x = mmul(mmul(u3, den, M), winv, M);               // u^3 / v^3
-  const u64 a24 = mmul(mmul(num, v3, M), winv, M);             // (A + 2) / 4
+  const u64 x = Ar::mul(Ar::mul(u3, den, M), winv, M);         // u^3 / v^3
+  const u64 a24 = Ar::mul(Ar::mul(num, v3, M), winv, M);       // (A + 2) / 4
   // --- stage 1: Q = [k](x : 1), ladder from the top bit of k
-  XZ R0{x, M.one}, R1 = ecm_dbl(R0, a24, M);
+  XZ R0{x, M.one}, R1 = ecm_dbl<Ar>(R0, a24, M);
   for (int i = ECM_K_BITS - 2; i >= 0; --i) {
     const bool b = (ECM_K[i >> 5] >> (i & 31)) & 1u;
     if (b) { const XZ t = R0; R0 = R1; R1 = t; }
-    R1 = ecm_add1(R0, R1, x, M);
-    R0 = ecm_dbl(R0, a24, M);
+    R1 = ecm_add1<Ar>(R0, R1, x, M);
+    R0 = ecm_dbl<Ar>(R0, a24, M);
     if (b) { const XZ t = R0; R0 = R1; R1 = t; }
   }
   const XZ Q = R0;
@@ -162,48 +168,48 @@ __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
   }
   if (poll()) return 0;
   // --- stage 2: baby steps [j]Q for odd j <= 31 (kept for j in ECM_J), giant step [60]Q
-  const XZ Q2 = ecm_dbl(Q, a24, M);
+  const XZ Q2 = ecm_dbl<Ar>(Q, a24, M);
   u64 bx[ECM_NJ], bz[ECM_NJ];
   bx[0] = Q.x; bz[0] = Q.z;
-  XZ prev = Q, cur = ecm_add(Q2, Q, Q, M);                     // [1], [3]
+  XZ prev = Q, cur = ecm_add<Ar>(Q2, Q, Q, M);                 // [1], [3]
   int nb = 1;
   XZ P29{0, 0};
   #pragma unroll
   for (int j = 3; j <= 29; j += 2) {                           // cur = [j]
     if (j % 3 != 0 && j % 5 != 0) { bx[nb] = cur.x; bz[nb] = cur.z; ++nb; }
     if (j == 29) P29 = cur;
-    const XZ nxt = ecm_add(cur, Q2, prev, M);                  // [j + 2]
+    const XZ nxt = ecm_add<Ar>(cur, Q2, prev, M);              // [j + 2]
     prev = cur; cur = nxt;
   }
-  const XZ G1 = ecm_add(cur, P29, Q2, M);                      // [31] + [29] = [60]
+  const XZ G1 = ecm_add<Ar>(cur, P29, Q2, M);                  // [31] + [29] = [60]
   // normalise the baby steps: xn[i] = X_j / Z_j (one inverse for all eight)
   u64 c[ECM_NJ];
   c[0] = bz[0];
   #pragma unroll
-  for (int i = 1; i < ECM_NJ; ++i) c[i] = mmul(c[i - 1], bz[i], M);
+  for (int i = 1; i < ECM_NJ; ++i) c[i] = Ar::mul(c[i - 1], bz[i], M);
   u64 inv = 0;
   if (!dead) {
     const u64 g = gcd64(c[ECM_NJ - 1], n);
     if (g != 1) { dead = true; if (g < n) found = g; }
-    else { inv = mont_inverse(c[ECM_NJ - 1], M); if (!inv) dead = true; }
+    else { inv = mont_inverse<Ar>(c[ECM_NJ - 1], M); if (!inv) dead = true; }
   }
   u64 xn[ECM_NJ];
   #pragma unroll
   for (int i = ECM_NJ - 1; i > 0; --i) {
-    xn[i] = mmul(bx[i], mmul(inv, c[i - 1], M), M);
-    inv = mmul(inv, bz[i], M);
+    xn[i] = Ar::mul(bx[i], Ar::mul(inv, c[i - 1], M), M);
+    inv = Ar::mul(inv, bz[i], M);
   }
-  xn[0] = mmul(bx[0], inv, M);
+  xn[0] = Ar::mul(bx[0], inv, M);
   // giant steps G_m = [60 m]Q, m = 1 .. ECM_M1
   u64 acc = M.one;
   XZ Gp = G1, G = G1;
   for (int m = 1; m <= ECM_M1; ++m) {
-    if (m == 2) G = ecm_dbl(G1, a24, M);
-    else if (m > 2) { const XZ t = ecm_add(G, G1, Gp, M); Gp = G; G = t; }
+    if (m == 2) G = ecm_dbl<Ar>(G1, a24, M);
+    else if (m > 2) { const XZ t = ecm_add<Ar>(G, G1, Gp, M); Gp = G; G = t; }
     const u32 mask = ECM_PAIRS[m - 1];
     #pragma unroll
     for (int i = 0; i < ECM_NJ; ++i)
-      if (mask & (1u << i)) acc = mmul(acc, submod(G.x, mmul(xn[i], G.z, M), n), M);
+      if (mask & (1u << i)) acc = Ar::mul(acc, Ar::sub(G.x, Ar::mul(xn[i], G.z, M), M), M);
     if (m % ECM_STAGE2_POLL == 0 && poll()) return 0;
   }
   if (!dead) found = proper_gcd(acc, n);

@@ -637,6 +637,9 @@ __device__ __forceinline__ void put_record(const TailParams &T, const RecDev &r)
 #define ES_RUNG_WARPS 4
 #endif
 constexpr int RUNG_WARPS = ES_RUNG_WARPS;
+#ifndef ES_RUNG_TAIL_PER_BLOCK
+#define ES_RUNG_TAIL_PER_BLOCK RUNG_WARPS     // primes per block left for the block phase
+#endif
 #ifndef ES_RUNG_MIN_BLOCKS
 #define ES_RUNG_MIN_BLOCKS (16 / RUNG_WARPS)   // resident blocks per SM the register budget allows
 #endif
@@ -682,7 +685,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   HardBoard B;
   B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
-  const u64 tail = min(n, (u64)gridDim.x * RUNG_WARPS);
+  const u64 tail = min(n, (u64)gridDim.x * ES_RUNG_TAIL_PER_BLOCK);
   const u64 nw = n - tail;                           // primes [0, nw): a warp each
   for (;;) {
     u64 i = 0;

@@ -72,10 +72,11 @@ __device__ inline bool warp_is_prime(u64 n, u32 lane) {
 // Brent's backtrack from ys: step one at a time until gcd(|x - ys|, n) > 1 (bounded by the
 // longest batch).
 constexpr u32 RHO_BATCH_MAX_BACKTRACK = 512;
+template <class Ar>
 __device__ __forceinline__ u64 rho_backtrack(u64 x, u64 ys, u64 cm, u64 n, const Mont &M) {
   u64 g = 1;
   for (u32 guard = 0; g == 1 && guard <= RHO_BATCH_MAX_BACKTRACK; ++guard) {
-    ys = addmod(mmul(ys, ys, M), cm, n);
+    ys = Ar::add(Ar::mul(ys, ys, M), cm, M);
     const u64 diff = x > ys ? x - ys : ys - x;
     g = gcd64(diff ? diff : n, n);
   }
@@ -148,8 +149,9 @@ __device__ __forceinline__ u32 ld_volatile(const unsigned int *p) { return *(con
 
 // The lockstep walk shared by the owner and its helpers. c0: this lane's first constant,
 // cstep: the distance to its next one. poll() is called by every lane between batches (warp-
-// uniform) and returns a divisor handed in from outside, ~0 to stop, or 0 to go on.
-template <class Poll>
+// uniform) and returns a divisor handed in from outside, ~0 to stop, or 0 to go on. Ar is the
+// arithmetic (es_arith.cuh): LazyArith for n < 2^62, ExactArith above.
+template <class Ar, class Poll>
 __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep, u64 budget, u32 lane, Poll poll,
                                         u64 r0 = RHO_R0) {
   const u64 y0 = to_mont(2, M);
@@ -160,14 +162,14 @@ __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep,
   for (u64 r = r0;; r <<= 1) {
     x = y;
     if (steps + 2 * r > budget) return 0;
-    for (u64 i = 0; i < r; ++i) y = addmod(mmul(y, y, M), cm, n);
+    for (u64 i = 0; i < r; ++i) y = Ar::add(Ar::mul(y, y, M), cm, M);
     steps += r;
     for (u64 k = 0; k < r; k += RHO_BATCH) {
       ys = y;
       const u64 lim = RHO_BATCH < r - k ? RHO_BATCH : r - k;
       for (u64 i = 0; i < lim; ++i) {
-        y = addmod(mmul(y, y, M), cm, n);
-        q = mmul(q, x > y ? x - y : y - x, M);        // a closed cycle makes q 0
+        y = Ar::add(Ar::mul(y, y, M), cm, M);
+        q = Ar::mul(q, x > y ? x - y : y - x, M);     // a closed cycle makes q = 0 mod n
       }
       steps += lim;
       u64 mine = 0;
@@ -175,7 +177,7 @@ __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep,
       if (g != 1) {
         if (g != n) mine = g;
         else {
-          const u64 gb = rho_backtrack(x, ys, cm, n, M);
+          const u64 gb = rho_backtrack<Ar>(x, ys, cm, n, M);
           if (gb != 1 && gb != n) mine = gb;
           else {                                        // this walk is spent: next constant
             c += cstep;
@@ -196,11 +198,11 @@ __device__ __forceinline__ u64 rho_walk(u64 n, const Mont &M, u64 c0, u64 cstep,
 // returns what rho_walk's does (a divisor handed in, ~0 to stop, 0 to go on); a nonzero answer
 // ends the round and is left in ext. Returns the first divisor a lane found (the same value in
 // every lane), or 0.
-template <class Poll>
+template <class Ar, class Poll>
 __device__ inline u64 warp_ecm(const Mont &M, u64 sigma0, u32 lane, Poll poll, u64 &ext) {
   ext = 0;
   auto p = [&]() -> bool { ext = poll(); return ext != 0; };
-  const u64 d = ecm_curve(sigma0 + lane, M, p);
+  const u64 d = ecm_curve<Ar>(sigma0 + lane, M, p);
   const unsigned has = __ballot_sync(FULL, d != 0);
   return has ? __shfl_sync(FULL, d, __ffs(has) - 1) : 0;
 }
@@ -244,20 +246,27 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
     return ext;
   };
   // Brent's rho first; a cofactor it has not split goes to ECM rounds (charged against the same
-  // budget), and rho resumes with fresh constants for whatever budget remains after them.
-  const bool ecm = budget >= ECM_AFTER + ECM_ROUND_STEPS;
-  u64 f = rho_walk(n, M, 1 + lane, 32, ecm ? ECM_AFTER : budget, lane, poll);
-  if (!f && !stop && ecm) {
-    u64 steps = ECM_AFTER;
-    u64 ext = poll(RHO_POST_STEPS > steps ? RHO_POST_STEPS : steps);   // post n to the board now
-    if (ext && ext != ~0ull) f = ext;
-    for (u32 round = 0; !f && !stop && round < ECM_OWNER_ROUNDS && steps + ECM_ROUND_STEPS <= budget; ++round) {
-      f = warp_ecm(M, ECM_SIGMA_OWNER + 32 * (u64)round, lane, [&]() -> u64 { return poll(steps); }, ext);
-      steps += ECM_ROUND_STEPS;
-      if (!f && ext && ext != ~0ull) f = ext;
+  // budget), and rho resumes with fresh constants for whatever budget remains after them. Every
+  // stage-D cofactor is below 2^62 (A = (p + r)/4 with p below 2^64) and takes the lazy
+  // arithmetic; larger n (factorization probes only) walk rho in exact arithmetic, without ECM.
+  u64 f = 0;
+  if (n >= LazyArith::NMAX) {
+    f = rho_walk<ExactArith>(n, M, 1 + lane, 32, budget, lane, poll);
+  } else {
+    const bool ecm = budget >= ECM_AFTER + ECM_ROUND_STEPS;
+    f = rho_walk<LazyArith>(n, M, 1 + lane, 32, ecm ? ECM_AFTER : budget, lane, poll);
+    if (!f && !stop && ecm) {
+      u64 steps = ECM_AFTER;
+      u64 ext = poll(RHO_POST_STEPS > steps ? RHO_POST_STEPS : steps);   // post n to the board now
+      if (ext && ext != ~0ull) f = ext;
+      for (u32 round = 0; !f && !stop && round < ECM_OWNER_ROUNDS && steps + ECM_ROUND_STEPS <= budget; ++round) {
+        f = warp_ecm<LazyArith>(M, ECM_SIGMA_OWNER + 32 * (u64)round, lane, [&]() -> u64 { return poll(steps); }, ext);
+        steps += ECM_ROUND_STEPS;
+        if (!f && ext && ext != ~0ull) f = ext;
+      }
+      if (!f && !stop && steps < budget)
+        f = rho_walk<LazyArith>(n, M, 1 + lane + 32 * 1024, 32, budget - steps, lane, poll);
     }
-    if (!f && !stop && steps < budget)
-      f = rho_walk(n, M, 1 + lane + 32 * 1024, 32, budget - steps, lane, poll);
   }
   if (lane == 0 && slot >= 0 && slot < (int)HARD_SLOTS) {  // take n off the board
     atomicExch(&board->slot[slot].state, 1u);
@@ -312,7 +321,8 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
     // a restart adds 2^25); a posted cofactor has already outlasted its owner's first walks, so
     // helpers start with a longer window
     const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
-    const u64 d = rho_walk(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
+    const u64 d = n < LazyArith::NMAX ? rho_walk<LazyArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0)
+                                      : rho_walk<ExactArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
     if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
       atomicCAS(&hs->found, 0ull, (unsigned long long)d);
     __syncwarp();

@@ -1,8 +1,10 @@
 // Host build of the device ECM (erdos-strauss_gb300/csrc/es_ecm.cuh) for the CPU tests: the
 // same source compiled by g++ with the four device intrinsics it uses defined on 128-bit host
-// integers. Checks the binary inverse on random residues, then runs 32 curves (sigma 6..37,
-// one warp's first round) on seeded semiprimes with prime factors of 18-31 bits and prints the
-// fraction of curves that split each size; every divisor returned must divide n properly.
+// integers. Checks the binary inverse on random residues and the lazy Montgomery multiply
+// against exact residues, then runs 32 curves (sigma 6..37, one warp's first round) on seeded
+// 62-bit semiprimes with prime factors of 18-31 bits in the lazy arithmetic the engine uses
+// and prints the fraction of curves that split each size; the exact arithmetic must find the
+// same divisors curve for curve, and every divisor returned must divide n properly.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -54,6 +56,17 @@ int main(int argc, char **argv) {
       return 1;
     }
   }
+  for (int t = 0; t < 200000; ++t) {
+    const u64 n = (g() >> 2) | 1;
+    if (n < 3) continue;
+    const Mont M = mont_init(n);
+    const u64 a = g() % (2 * n), b = g() % (2 * n);
+    const u64 r = LazyArith::mul(a, b, M);
+    if (r >= 2 * n || r % n != mmul(a % n, b % n, M)) {
+      printf("FAIL lazy multiply a=%llu b=%llu n=%llu\n", a, b, n);
+      return 1;
+    }
+  }
   for (int bits = 18; bits <= 31; ++bits) {
     int split = 0, curves = 0, warps = 0;
     for (int t = 0; t < trials; ++t) {
@@ -61,7 +74,11 @@ int main(int argc, char **argv) {
       const Mont M = mont_init(n);
       bool any = false;
       for (u64 lane = 0; lane < 32; ++lane, ++curves) {
-        const u64 d = ecm_curve(6 + lane, M, [] { return false; });
+        const u64 d = ecm_curve<LazyArith>(6 + lane, M, [] { return false; });
+        if (d != ecm_curve<ExactArith>(6 + lane, M, [] { return false; })) {
+          printf("FAIL lazy and exact curves differ n=%llu sigma=%llu\n", n, 6 + lane);
+          return 1;
+        }
         if (!d) continue;
         if (d <= 1 || d >= n || n % d) {
           printf("FAIL divisor %llu of %llu\n", d, n);
