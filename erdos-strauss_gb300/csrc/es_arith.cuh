@@ -148,6 +148,26 @@ __device__ __forceinline__ bool sprp_mont(u64 bm, u64 d, int s, const Mont &M) {
   return false;
 }
 
+// The same round in an arithmetic policy (LazyArith needs n < 2^62): the comparisons take the
+// exact representative.
+template <class Ar>
+__device__ __forceinline__ bool sprp_ar(u64 bm, u64 d, int s, const Mont &M) {
+  const u64 mone = M.n - M.one;
+  u64 x = M.one, b = bm, e = d;
+  while (e) {
+    if (e & 1) x = Ar::mul(x, b, M);
+    b = Ar::mul(b, b, M);
+    e >>= 1;
+  }
+  x = Ar::norm(x, M);
+  if (x == M.one || x == mone) return true;
+  for (int i = 1; i < s; ++i) {
+    x = Ar::norm(Ar::mul(x, x, M), M);
+    if (x == mone) return true;
+  }
+  return false;
+}
+
 __constant__ const u64 MR_BASES[12] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
 
 // The reference's is_prime: trial division by the 12 bases, then all 12 SPRP rounds

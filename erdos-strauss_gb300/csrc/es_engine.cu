@@ -852,6 +852,7 @@ struct Slot {
   u32 *d_primes = nullptr, *d_direct = nullptr, *d_cand = nullptr;
   RecDev *d_recs = nullptr;
   size_t cap = 0;
+  size_t rec_prefix = 0;                // records the captured graph copies back itself
   unsigned long long *d_ctr = nullptr;  // [0] queue [1] surv [2] prime [3] direct [4] rec [5] cand
                                       // [6] rung queue (blocks) [7] rungs done [8] help sessions
                                       // [9] rung queue (warps), board at [16]
@@ -1171,15 +1172,22 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
 
 // The persistent schedule as a CUDA graph: counters cleared, the whole staging area copied,
 // every kernel, and the counters copied back, captured once and replayed per batch.
+constexpr size_t REC_PREFIX = 4096;
+
 static es_status capture_graph(es_engine *e, Slot *sl) {
   drop_graph(sl);
   CU(cudaStreamBeginCapture(sl->stream, cudaStreamCaptureModeThreadLocal));
   es_status s = ES_OK;
   const cudaError_t m = cudaMemsetAsync(sl->d_cnt, 0, sl->win_cap * sizeof(WinCount), sl->stream);
   if (m == cudaSuccess) s = enqueue_funnel(e, sl, true, sl->d_cnt, sl->win_cap, sl->shortw_cap, 0, true);
+  // The graph also copies back the first REC_PREFIX record slots, so that a batch with fewer
+  // records (every 4096-window batch at 1e19 has about 1.6 K) needs no copy after the run.
+  sl->rec_prefix = std::min<size_t>(sl->cap, REC_PREFIX);
   if (m == cudaSuccess && s == ES_OK) {
-    const cudaError_t c2 = cudaMemcpyAsync(sl->h_cnt, sl->d_cnt, sl->win_cap * sizeof(WinCount),
-                                           cudaMemcpyDeviceToHost, sl->stream);
+    cudaError_t c2 = cudaMemcpyAsync(sl->h_cnt, sl->d_cnt, sl->win_cap * sizeof(WinCount),
+                                     cudaMemcpyDeviceToHost, sl->stream);
+    if (c2 == cudaSuccess)
+      c2 = cudaMemcpyAsync(sl->h_recs, sl->d_recs, sl->rec_prefix * sizeof(RecDev), cudaMemcpyDeviceToHost, sl->stream);
     if (c2 != cudaSuccess) s = fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(c2));
   }
   cudaGraph_t g = nullptr;
@@ -1244,6 +1252,7 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
     u64 launches = 0, surv_max = 0, surv_total = 0, prime_total = 0;
     u32 status = 0;
     hr.clear();
+    size_t have_recs = 0;                 // records already on the host (the graph's prefix copy)
     auto collect = [&]() -> es_status {   // after a pass: timings, counts, records
       prep_ms += ev_ms(sl->ev[0], sl->ev[7]); short_ms += ev_ms(sl->ev[7], sl->ev[8]);
       long_ms += ev_ms(sl->ev[8], sl->ev[1]);
@@ -1255,11 +1264,13 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
       status |= *sl->h_status;
       if (ctr[1] > sl->cap) return ES_OK;
       const size_t nrec = (size_t)std::min<u64>(ctr[4], sl->cap);
-      if (nrec) {
-        CU(cudaMemcpyAsync(sl->h_recs, sl->d_recs, nrec * sizeof(RecDev), cudaMemcpyDeviceToHost, sl->stream));
+      const size_t have = std::min(nrec, have_recs);
+      if (nrec > have) {
+        CU(cudaMemcpyAsync(sl->h_recs + have, sl->d_recs + have, (nrec - have) * sizeof(RecDev),
+                           cudaMemcpyDeviceToHost, sl->stream));
         CU(cudaStreamSynchronize(sl->stream));
-        hr.insert(hr.end(), sl->h_recs, sl->h_recs + nrec);
       }
+      if (nrec) hr.insert(hr.end(), sl->h_recs, sl->h_recs + nrec);
       return ES_OK;
     };
     if (persistent) {
@@ -1291,6 +1302,7 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
       CU(cudaStreamSynchronize(sl->stream));
       device_ms = ms_since(t_launch);
       launches = 7;
+      have_recs = sl->rec_prefix;
       s = collect();
       if (s) return s;
     } else {
@@ -1346,16 +1358,26 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
     o.survivors = c.unsolved;
   }
   if (recs) {
-    std::sort(hr.begin(), hr.end(), [](const RecDev &a, const RecDev &b) {
-      if (a.win != b.win) return a.win < b.win;
-      if (a.lane != b.lane) return a.lane < b.lane;
-      return a.J < b.J;
-    });
+    // Lane-major order within each window: a counting sort on the window index straight into
+    // the caller's buffer, then (lane, J) order inside each window's few records.
+    static_assert(sizeof(RecDev) == sizeof(es_record), "record layout");
     recs->n = hr.size();
     recs->recs = (es_record *)malloc(std::max<size_t>(hr.size(), 1) * sizeof(es_record));
     if (!recs->recs) return fail(e, ES_ERR_NOMEM, "host records");
-    static_assert(sizeof(RecDev) == sizeof(es_record), "record layout");
-    memcpy(recs->recs, hr.data(), hr.size() * sizeof(es_record));
+    RecDev *out = reinterpret_cast<RecDev *>(recs->recs);
+    std::vector<u32> start(n + 1, 0);
+    for (const RecDev &r : hr) ++start[std::min<size_t>(r.win, n - 1) + 1];
+    for (size_t i = 0; i < n; ++i) start[i + 1] += start[i];
+    std::vector<u32> pos(start.begin(), start.end() - 1);
+    for (const RecDev &r : hr) out[pos[std::min<size_t>(r.win, n - 1)]++] = r;
+    for (size_t i = 0; i < n; ++i) {
+      if (start[i + 1] - start[i] > 1)
+        std::sort(out + start[i], out + start[i + 1], [](const RecDev &a, const RecDev &b) {
+          if (a.win != b.win) return a.win < b.win;
+          if (a.lane != b.lane) return a.lane < b.lane;
+          return a.J < b.J;
+        });
+    }
   }
   sl->timing.host_setup_ms = setup_ms;
   sl->timing.host_device_ms = device_ms;

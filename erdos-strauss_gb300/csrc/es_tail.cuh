@@ -63,7 +63,8 @@ __device__ inline bool warp_is_prime(u64 n, u32 lane) {
       u64 d = n - 1;
       const int s = __ffsll((long long)d) - 1;
       d >>= s;
-      ok = sprp_mont(to_mont(b, M), d, s, M);
+      const u64 bm = to_mont(b, M);
+      ok = n < LazyArith::NMAX ? sprp_ar<LazyArith>(bm, d, s, M) : sprp_mont(bm, d, s, M);
     }
   }
   return __all_sync(FULL, ok);

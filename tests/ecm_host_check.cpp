@@ -1,7 +1,7 @@
 // Host build of the device ECM (erdos-strauss_gb300/csrc/es_ecm.cuh) for the CPU tests: the
 // same source compiled by g++ with the four device intrinsics it uses defined on 128-bit host
-// integers. Checks the binary inverse on random residues and the lazy Montgomery multiply
-// against exact residues, then runs 32 curves (sigma 6..37, one warp's first round) on seeded
+// integers. Checks the binary inverse on random residues, the lazy Montgomery multiply against
+// exact residues and the lazy strong-probable-prime round against the exact one, then runs 32 curves (sigma 6..37, one warp's first round) on seeded
 // 62-bit semiprimes with prime factors of 18-31 bits in the lazy arithmetic the engine uses
 // and prints the fraction of curves that split each size; the exact arithmetic must find the
 // same divisors curve for curve, and every divisor returned must divide n properly.
@@ -65,6 +65,21 @@ int main(int argc, char **argv) {
     if (r >= 2 * n || r % n != mmul(a % n, b % n, M)) {
       printf("FAIL lazy multiply a=%llu b=%llu n=%llu\n", a, b, n);
       return 1;
+    }
+  }
+  for (int t = 0; t < 20000; ++t) {                     // the lazy strong-probable-prime round
+    const u64 n = (t & 1) ? random_prime(40 + t % 22, g) : ((g() >> 2) | 1);
+    if (n < 41) continue;
+    const Mont M = mont_init(n);
+    u64 d = n - 1;
+    const int sh = __ffsll((long long)d) - 1;
+    d >>= sh;
+    for (u64 b : BASES) {
+      const u64 bm = to_mont(b, M);
+      if (sprp_ar<LazyArith>(bm, d, sh, M) != sprp_mont(bm, d, sh, M)) {
+        printf("FAIL lazy sprp n=%llu base=%llu\n", n, b);
+        return 1;
+      }
     }
   }
   for (int bits = 18; bits <= 31; ++bits) {
