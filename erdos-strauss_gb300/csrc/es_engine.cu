@@ -858,6 +858,18 @@ struct Slot {
                                       // [9] rung queue (warps), board at [16]
   u32 *d_status = nullptr;
   es_timing_t timing{};
+  struct HostScratch {                  // per-run host vectors, kept with their capacity
+    std::vector<WinDev> wd;
+    std::vector<ShortWin> shortw;
+    std::vector<u64> npos;
+    std::vector<RecDev> hr;
+    std::vector<u32> start, pos;
+    std::vector<uint8_t> mag;
+    std::vector<es_window> dw;          // the long-window split (run_windows)
+    std::vector<std::pair<u32, u64>> dmap;
+    std::vector<es_counters> pc;
+    std::vector<es_record> all;
+  } hs;
   std::mutex mu;                        // one run at a time per slot
 };
 
@@ -1234,16 +1246,18 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
     if (w[i].lo <= floor_)
       return fail(e, ES_ERR_RANGE, "LO must exceed max pmin of the filter table (" + std::to_string(floor_) + ")");
   }
-  std::vector<WinDev> wd;
-  std::vector<ShortWin> shortw;
+  std::vector<WinDev> &wd = sl->hs.wd;
+  std::vector<ShortWin> &shortw = sl->hs.shortw;
   const u64 total_items = describe(e, w, n, wd, shortw);
-  std::vector<u64> npos(n);
+  std::vector<u64> &npos = sl->hs.npos;
+  npos.resize(n);
   u64 positions_bound = 0;
   for (size_t i = 0; i < n; ++i) positions_bound += (npos[i] = positions_in(e, w[i].lo, w[i].hi));
   size_t cap = (size_t)std::min<u64>(std::max<u64>(positions_bound / 64, 1 << 16), 1ull << 26);
   cap = std::max(cap, sl->cap);
   const bool persistent = schedule == ES_SCHED_PERSISTENT;
-  std::vector<RecDev> hr;
+  std::vector<RecDev> &hr = sl->hs.hr;
+  hr.clear();
   bool done = false;
   for (int attempt = 0; attempt < 4 && !done; ++attempt) {
     es_status s = ensure_capacity(e, sl, n, cap);
@@ -1284,7 +1298,8 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
         // a counting sort on the work's binary order of magnitude (largest first, ties in
         // input order) is all the balance needs
         const size_t ns = shortw.size();
-        std::vector<uint8_t> mag(ns);
+        std::vector<uint8_t> &mag = sl->hs.mag;
+        mag.resize(ns);
         u32 start[34] = {0};
         for (size_t k = 0; k < ns; ++k) {
           const ShortWin &x = shortw[k];
@@ -1365,10 +1380,11 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
     recs->recs = (es_record *)malloc(std::max<size_t>(hr.size(), 1) * sizeof(es_record));
     if (!recs->recs) return fail(e, ES_ERR_NOMEM, "host records");
     RecDev *out = reinterpret_cast<RecDev *>(recs->recs);
-    std::vector<u32> start(n + 1, 0);
+    std::vector<u32> &start = sl->hs.start, &pos = sl->hs.pos;
+    start.assign(n + 1, 0);
     for (const RecDev &r : hr) ++start[std::min<size_t>(r.win, n - 1) + 1];
     for (size_t i = 0; i < n; ++i) start[i + 1] += start[i];
-    std::vector<u32> pos(start.begin(), start.end() - 1);
+    pos.assign(start.begin(), start.end() - 1);
     for (const RecDev &r : hr) out[pos[std::min<size_t>(r.win, n - 1)]++] = r;
     for (size_t i = 0; i < n; ++i) {
       if (start[i + 1] - start[i] > 1)
@@ -1410,10 +1426,12 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
   }
   if (!split) return run_device_windows(e, sl, w, n, schedule, per_window, recs);
   memset(per_window, 0, n * sizeof(es_counters));
-  std::vector<es_record> all;
+  std::vector<es_record> &all = sl->hs.all;
+  all.clear();
   es_timing_t tot{};
-  std::vector<es_window> dw;
-  std::vector<std::pair<u32, u64>> dmap;          // (window, position offset) per device window
+  std::vector<es_window> &dw = sl->hs.dw;
+  std::vector<std::pair<u32, u64>> &dmap = sl->hs.dmap;   // (window, position offset) per device window
+  std::vector<es_counters> &pc = sl->hs.pc;
   dw.reserve(PASS_WINDOWS);
   dmap.reserve(PASS_WINDOWS);
   // device windows are produced a pass at a time: (i, t) is the next sub-window to emit
@@ -1437,7 +1455,7 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
       if (hi - a <= step) { ++i; t = 0; } else ++t;
     }
     const size_t m = dw.size();
-    std::vector<es_counters> pc(m);
+    pc.resize(m);
     es_records pr{nullptr, 0};
     const es_status st = run_device_windows(e, sl, dw.data(), m, schedule, pc.data(), recs ? &pr : nullptr);
     if (st != ES_OK) { es_free_records(&pr); return st; }
@@ -1447,6 +1465,7 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
       o.positions += c.positions; o.covered += c.covered; o.sieved += c.sieved; o.mr += c.mr;
       o.composite += c.composite; o.rung += c.rung; o.direct += c.direct; o.survivors += c.survivors;
     }
+    all.reserve(all.size() + pr.n);
     for (size_t r = 0; r < pr.n; ++r) {
       es_record x = pr.recs[r];
       const auto &mp = dmap[x.window];
@@ -1466,11 +1485,19 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
   }
   sl->timing = tot;
   if (recs) {
-    std::sort(all.begin(), all.end(), [](const es_record &x, const es_record &y) {
-      if (x.window != y.window) return x.window < y.window;
-      if (x.lane != y.lane) return x.lane < y.lane;
-      return x.J < y.J;
-    });
+    // Each pass's records come in (device window, lane, J) order and the device windows of a
+    // window are consecutive (across passes too), so the records are already grouped by window
+    // in ascending order; only a split window's group needs putting back in (lane, J) order.
+    for (size_t a = 0; a < all.size();) {
+      size_t b = a + 1;
+      while (b < all.size() && all[b].window == all[a].window) ++b;
+      if (b - a > 1)
+        std::sort(all.begin() + a, all.begin() + b, [](const es_record &x, const es_record &y) {
+          if (x.lane != y.lane) return x.lane < y.lane;
+          return x.J < y.J;
+        });
+      a = b;
+    }
     recs->n = all.size();
     recs->recs = (es_record *)malloc(std::max<size_t>(all.size(), 1) * sizeof(es_record));
     if (!recs->recs) return fail(e, ES_ERR_NOMEM, "host records");
