@@ -188,15 +188,22 @@ __device__ inline bool is_prime64(u64 n) {
   return true;
 }
 
-// Base-2 SPRP (sieve/rung_scan3.cpp:680-689) on an odd n > 2.
+// Base-2 SPRP (sieve/rung_scan3.cpp:680-689) on an odd n > 2. The base is 2 = one + one in
+// Montgomery form, so r2 (64 doublings) is not needed; below 2^62 the round runs in the lazy
+// arithmetic.
 __device__ inline bool sprp2_64(u64 n) {
   if (n < 2) return false;
   if (!(n & 1)) return n == 2;
-  const Mont M = mont_init(n);
+  Mont M;
+  M.n = n;
+  M.ninv = 0 - inv_pow2(n);
+  M.one = (0 - n) % n;
+  M.r2 = 0;
   u64 d = n - 1;
   const int s = __ffsll((long long)d) - 1;
   d >>= s;
-  return sprp_mont(addmod(M.one, M.one, n), d, s, M);
+  const u64 two = addmod(M.one, M.one, n);
+  return n < LazyArith::NMAX ? sprp_ar<LazyArith>(two, d, s, M) : sprp_mont(two, d, s, M);
 }
 
 // ---------------------------------------------------------------- gcd, isqrt
