@@ -45,6 +45,7 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 MARK_SHORT_TRAFFIC_4096 = 79.559680e6 + 2.436608e6
 MARK_SHORT_ALG_4096 = 79280448               # the same launch's algorithmic bytes
 MARK_SHORT_INST_4096 = 823032516             # smsp__inst_executed.sum of the same capture
+RUNG_INST_4096 = 120287003                   # smsp__inst_executed.sum of one k_rung launch, same workload
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
 MARKS_PER_INTEGER_GPU = 9.0951 / (2042040 / 2308)
@@ -444,6 +445,17 @@ def run_gpu(args, ws, rank, local):
         roof["marks"] = {"per_launch": marks, "achieved": marks / (per_launch_ms / 1000.0), "unit": "marks/s",
                          "rmw_equivalent_gbs": rmw_gbs, "smem_peak_gbs": smem_peak, "peak_kind": "nominal",
                          "frac": rmw_gbs / smem_peak}
+    if args.windows == 4096 and args.sieve == 0 and stage["rung_ms"] > 0:
+        # The survivor tail (stage D): integer-pipe work bound by the latency of its hardest
+        # factorizations. Warp instructions of one k_rung launch (ncu smsp__inst_executed.sum on
+        # this workload) over its live time, against the same peak issue rate.
+        rung_launch_ms = stage["rung_ms"] / args.steps
+        mhz = clocks.get("sm_mhz") or 2070.0
+        peak_issue = 152 * 4 * mhz * 1e6
+        rate = RUNG_INST_4096 / (rung_launch_ms / 1000.0)
+        roof["stage_d"] = {"kernel": "k_rung", "bound": "latency", "ms_per_launch": rung_launch_ms,
+                           "issue": {"achieved": rate, "peak": peak_issue, "unit": "warp inst/s",
+                                     "frac": rate / peak_issue, "inst_per_launch": RUNG_INST_4096}}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
