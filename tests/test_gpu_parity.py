@@ -232,6 +232,35 @@ def test_factorization_battery():
         assert f == oracle.factor(v), v
 
 
+def test_factorization_ecm_range():
+    """Cofactors below 2^62 go through rho and then the lazy-arithmetic ECM rounds, those from
+    2^62 up through exact rho: balanced semiprimes of 20-31-bit primes, pairs straddling the
+    2^62 switch, and three-prime products, against the oracle's factorization."""
+    g = workloads.SplitMix64(62)
+    def nextp(a):
+        while not oracle.is_prime(a):
+            a += 1
+        return a
+    vals = []
+    for bits in range(20, 32):
+        for _ in range(6):
+            a = nextp((1 << (bits - 1)) + g.next() % (1 << (bits - 1)))
+            b = nextp((1 << (61 - bits)) + g.next() % (1 << (61 - bits)))
+            vals.append(a * b)
+    for _ in range(12):                                  # around 2^62
+        a = nextp(2147483648 + g.next() % 2147483648)
+        b = nextp((1 << 62) // a - 2000 + g.next() % 4000)
+        vals.append(a * b)
+    for _ in range(12):
+        a, b = nextp(65537 + g.next() % 1000000), nextp(65537 + g.next() % 1000000)
+        c = nextp(65537 + g.next() % ((1 << 62) // (a * b) - 65537))
+        vals.append(a * b * c)
+    assert any(v < 1 << 62 for v in vals) and any(v >= 1 << 62 for v in vals)
+    got = engine().factor(vals)
+    for v, f in zip(vals, got):
+        assert f == oracle.factor(v), v
+
+
 def _primes_at(height, count):
     out, p = [], height | 1
     while len(out) < count:
