@@ -360,7 +360,7 @@ def run_gpu(args, ws, rank, local):
     dev_ms, wall_s, launches, recs_n, items = 0.0, 0.0, 0, 0, 0
     stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
     kern = {"prep_ms": 0.0, "mark_short_ms": 0.0, "mark_long_ms": 0.0}
-    host = {"host_setup_ms": 0.0, "host_device_ms": 0.0, "host_collect_ms": 0.0}
+    host = {"host_setup_ms": 0.0, "host_device_ms": 0.0, "host_collect_ms": 0.0, "host_total_ms": 0.0}
     warr, carr = eng.make_windows(wins), eng.make_counters(len(wins))
     with Clocks(local) as clk:
         for _ in range(args.steps):

@@ -1954,10 +1954,13 @@ es_status es_run_window(es_engine *e, uint64_t lo, uint64_t hi, es_counters *out
   if (!e || !out) return ES_ERR_ARG;
   std::lock_guard<std::mutex> lk(e->slots[0].mu);
   cudaSetDevice(e->device);
+  const auto t0 = std::chrono::steady_clock::now();
   es_window w{lo, hi};
   memset(out, 0, sizeof *out);
   if (recs) { recs->recs = nullptr; recs->n = 0; }
-  return run_windows(e, &e->slots[0], &w, 1, ES_SCHED_PERSISTENT, out, recs);
+  const es_status st = run_windows(e, &e->slots[0], &w, 1, ES_SCHED_PERSISTENT, out, recs);
+  e->slots[0].timing.host_total_ms = ms_since(t0);
+  return st;
 }
 
 es_status es_run_batch(es_engine *e, const es_window *w, size_t n, int schedule, es_counters *per_window,
@@ -1965,11 +1968,14 @@ es_status es_run_batch(es_engine *e, const es_window *w, size_t n, int schedule,
   if (!e || (!w && n) || !per_window) return ES_ERR_ARG;
   if (schedule != ES_SCHED_PLAIN && schedule != ES_SCHED_PERSISTENT) return ES_ERR_ARG;
   std::lock_guard<std::mutex> lk(e->slots[0].mu);
+  const auto t0 = std::chrono::steady_clock::now();
   cudaSetDevice(e->device);
   memset(per_window, 0, n * sizeof(es_counters));
   if (recs) { recs->recs = nullptr; recs->n = 0; }
   if (n == 0) return ES_OK;
-  return run_windows(e, &e->slots[0], w, n, schedule, per_window, recs);
+  const es_status st = run_windows(e, &e->slots[0], w, n, schedule, per_window, recs);
+  e->slots[0].timing.host_total_ms = ms_since(t0);
+  return st;
 }
 
 es_status es_free_records(es_records *r) {

@@ -84,7 +84,7 @@ class Timing(C.Structure):
                                           "mark_short_ms", "mark_long_ms")] + \
                [(n, C.c_uint64) for n in ("marks_kernel_launches", "kernel_launches", "mark_items", "survivors",
                                           "primes", "short_pairs", "mask_bytes")] + \
-               [(n, C.c_double) for n in ("host_setup_ms", "host_device_ms", "host_collect_ms")]
+               [(n, C.c_double) for n in ("host_setup_ms", "host_device_ms", "host_collect_ms", "host_total_ms")]
 
 
 _lib = None

@@ -126,8 +126,11 @@ typedef struct {
   uint64_t short_pairs;     /* (lane, short window) pairs, active or not, walked by k_mark_short */
   uint64_t mask_bytes;      /* kill-mask table bytes one k_mark_short launch reads */
   /* host wall time of the call: describing and staging the windows, from the launch to the
-   * end of the device work (copies included), and collecting counters and records */
-  double host_setup_ms, host_device_ms, host_collect_ms;
+   * end of the device work (copies included), and collecting counters and records; and the
+   * whole es_run_batch / es_run_window call inside the library (with the long-window split,
+   * the three above are summed over its passes and host_total_ms also holds the split's own
+   * work) */
+  double host_setup_ms, host_device_ms, host_collect_ms, host_total_ms;
 } es_timing_t;
 
 /* Batch schedules: per-window launches of the same kernels, or one persistent launch over
