@@ -1407,7 +1407,8 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
 // they keep one device window each and go to the segment marking. Sub-window t of a window
 // starts t * short_max positions into every lane, so its records map back to the window by
 // J += t * short_max, and its counters add up to the window's (every counter is a sum over
-// positions). Device windows are run in passes of at most PASS_WINDOWS.
+// positions). Device windows are run in passes of at most PASS_WINDOWS. Every caller passes
+// per_window zeroed.
 constexpr size_t PASS_WINDOWS = 1u << 18;
 
 static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t n, int schedule,
@@ -1425,7 +1426,6 @@ static es_status run_windows(es_engine *e, Slot *sl, const es_window *w, size_t 
     if (e->sched.long_split && schedule == ES_SCHED_PERSISTENT && len > S * M) split = true;
   }
   if (!split) return run_device_windows(e, sl, w, n, schedule, per_window, recs);
-  memset(per_window, 0, n * sizeof(es_counters));
   std::vector<es_record> &all = sl->hs.all;
   all.clear();
   es_timing_t tot{};
