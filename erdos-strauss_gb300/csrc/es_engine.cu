@@ -276,7 +276,10 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 // warp takes one short window at a time and marks the segments of those lanes in it. The
 // per-window work that does not depend on the lane -- the stride descriptor and the
 // segment-start residue (lo / M) mod s -- is done once for all SHORT_LANES lanes.
-constexpr int SHORT_LANES = 2;
+#ifndef ES_SHORT_LANES
+#define ES_SHORT_LANES 2
+#endif
+constexpr int SHORT_LANES = ES_SHORT_LANES;
 constexpr u32 SMD_MAX = 512;       // stride descriptors staged in shared memory
 
 
@@ -526,13 +529,13 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
     auto load_q0 = [&](u32 wi) {
       return lane < P.nm_cov ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + d_first) : 0u;
     };
-    static_assert(SHORT_LANES == 2 && SEG_SMALL < 512, "n and b of two lanes are packed in one word");
+    static_assert(SHORT_LANES <= 3 && SEG_SMALL < 256, "n (8 bits) and b of each lane are packed in one word");
     for (u32 t0 = 0; warp + WS * t0 < nshort; t0 += 32) {
       const u32 my = warp + WS * (t0 + lane);
       uint4 x = make_uint4(0, 0, 0, 0), y = make_uint4(0, 0, 0, 0);
       if (my < nshort) { x = __ldg(sw4 + 2 * (size_t)my); y = __ldg(sw4 + 2 * (size_t)my + 1); }
       // fields: x = {Q lo, Q hi, lomod, wi}, y = {la, lb, lq, lr}
-      u32 pk = 0;                                  // n0 | n1 << 9 | b0 << 18 | b1 << 19
+      u32 pk = 0;                                  // n_q at bit 8q, b_q at bit 24 + q
       if (my < nshort) {
         #pragma unroll
         for (int q = 0; q < SHORT_LANES; ++q) {
@@ -541,10 +544,10 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
           const u32 bq = r < x.z ? 1u : 0u;
           const u32 d = r + (bq ? (u32)P.M : 0u) - x.z;              // (rho - lo) mod M
           const u32 nq = (l < P.L && l >= y.x && l < y.y) ? y.z + (d < y.w ? 1u : 0u) : 0u;
-          pk |= (nq << (9 * q)) | (bq << (18 + q));
+          pk |= (nq << (8 * q)) | (bq << (24 + q));
         }
       }
-      unsigned todo = __ballot_sync(FULL, (pk & 0x3FFFFu) != 0);
+      unsigned todo = __ballot_sync(FULL, (pk & ((1u << (8 * SHORT_LANES)) - 1)) != 0);
       u32 q0n = todo ? load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1)) : 0u;
       while (todo) {
         const int j = __ffs(todo) - 1;
@@ -553,9 +556,13 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
         const u32 wi = __shfl_sync(FULL, x.w, j);
         const u32 q0_first = q0n;
         if (todo) q0n = load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1));
-        const u32 n[SHORT_LANES] = {pj & 511u, (pj >> 9) & 511u};
-        const u32 b[SHORT_LANES] = {(pj >> 18) & 1u, (pj >> 19) & 1u};
-        const u32 nmax = max(n[0], n[1]);
+        u32 n[SHORT_LANES], b[SHORT_LANES], nmax = 0;
+        #pragma unroll
+        for (int q = 0; q < SHORT_LANES; ++q) {
+          n[q] = (pj >> (8 * q)) & 255u;
+          b[q] = (pj >> (24 + q)) & 1u;
+          nmax = max(nmax, n[q]);
+        }
         const WinRef R{wi, x.x, x.y, j};
         // chunks per lane; one chunk is by far the commonest case, so it is tested first.
         const u32 nc = (nmax + 31) >> 5;
