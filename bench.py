@@ -353,7 +353,7 @@ def run_gpu(args, ws, rank, local):
     eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local, sieve_p=args.sieve)
     wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
     n_int = integers(wins)
-    schedule = eng.autotune(wins, repeats=2) if not args.no_autotune else eng.schedule()
+    schedule = eng.autotune(wins, repeats=6) if not args.no_autotune else eng.schedule()
     for _ in range(args.warmup):
         eng.run_batch(wins)
     barrier(ws)

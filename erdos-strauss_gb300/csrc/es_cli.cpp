@@ -532,7 +532,7 @@ int main(int argc, char **argv) {
           (unsigned long long)(info.n_filters - info.n_certified));
   if (autotune) {
     es_schedule sc;
-    const es_status a = es_autotune(e, wins.data(), wins.size(), 2, &sc);
+    const es_status a = es_autotune(e, wins.data(), wins.size(), 6, &sc);
     if (a != ES_OK) {
       fprintf(stderr, "FATAL: autotune: %s: %s\n", es_status_str(a), es_last_error(e));
       es_close(e);

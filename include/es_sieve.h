@@ -205,7 +205,7 @@ es_status es_set_schedule(es_engine *engine, const es_schedule *s);
 /* Autotuner: runs the windows (persistent schedule) under each candidate schedule -- short_max
  * in {limit/4, limit/2, limit} x rung_blocks_per_sm in {4, 6, 8} x long_split in {1, 0} -- once to warm up
  * and `repeats` times
- * timed, keeps the best device time of each, checks that every candidate gave identical
+ * timed, keeps the mean device time of each, checks that every candidate gave identical
  * counters and records (ES_ERR_DEVICE_STATUS if not), and sets the fastest. `chosen` may be
  * null. */
 es_status es_autotune(es_engine *engine, const es_window *w, size_t n, int repeats, es_schedule *chosen);
