@@ -5,19 +5,32 @@
 //   K0[L][ldk]        u16  per (lane, filter): the residue K0 = K mod s at which filter f
 //                          kills lane l (p = rho_l + M*K), or K0_MISS; 2308 x 3752 x 2 B
 //                          = 17.3 MB for the M = 2042040 table, read coalesced row by row
-//   fdesc[nf], sdist  u32  stride s = mod/gcd(M,mod) per filter, and the distinct strides
+//   mtab[L][Wpad]     u64  per lane, one kill mask per distinct stride s: bit x set when some
+//                          filter of stride s kills K = x (mod s), for x < s + SEG_SMALL
+//                          (33.4 KB a lane, 77 MB for the M = 2042040 table)
+//   mdesc             per masked stride (densest first): s, its Qm column, its mask offset
+//   fdesc[nf]         u32  per filter: stride s = mod/gcd(M,mod) and its Qm column
 //   tdp/tde                trial-division table: 6541 odd primes < 2^16 with inverses
-// Per run: window descriptors, the survivor list, prime/direct index lists, records.
+// Per run: window and short-window descriptors, Qm[window][stride] = (lo / M) mod s, the
+// survivor list, prime/direct index lists, records, counters and the hard board.
 //
-// Pipeline per run (one CUDA stream):
-//   k_mark    one CTA per (window, lane, segment) item: a byte per position in shared
-//             memory, each filter clears its progression j = off, off+s, ... (plain byte
-//             stores: clearing is idempotent, so no atomics), popcount, warp-aggregated
-//             compaction of survivors (ballot/popc prefix) into the survivor list
-//   k_mr      one thread per survivor: base-2 SPRP then the 12-base Miller-Rabin
-//   k_rung    one thread per prime: the rung walk with device factorization
-//   k_direct  one thread per prime left over: the direct search, else SURVIVOR
-// Records come back unordered and the host sorts them by (window, lane, J): the
+// Pipeline per run (one CUDA stream, replayed as a CUDA graph for batches):
+//   k_prep        Qm for every window and stride
+//   k_mark_short  a CTA per pair of lanes with their mask rows in shared memory; each warp
+//                 walks short windows (and 128-position pieces of long ones): rounds of 32
+//                 strides, one funnel-shift extraction of 32 positions per stride and chunk,
+//                 a warp OR, stopping when every position is dead; survivors appended
+//   k_mark        the alternative for long windows: a byte map per segment in shared memory,
+//                 each filter clears its progression, warp-aggregated compaction
+//   k_mr          a thread per survivor: the base-2 strong-probable-prime round
+//   k_mr2         a warp per number that passed base 2: the 12-base test, one base per lane
+//   k_rung        stage D: a warp per prime while primes outnumber the grid's warps, then a
+//                 block of four warps per prime over successive rungs; warp trial division,
+//                 Miller-Rabin, Brent's rho, ECM rounds (es_tail.cuh, es_ecm.cuh), the rung
+//                 DP, and the exact certificate check (es_check.cuh) before a record is
+//                 written
+//   k_direct      a thread per prime left over: the direct search, else SURVIVOR
+// Records come back unordered; the host puts them in (window, lane, J) order, the
 // reference's lane-major order per window.
 #include "../../include/es_sieve.h"
 #include "es_arith.cuh"
