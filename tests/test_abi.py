@@ -129,3 +129,38 @@ def test_cli_dump_classes_2042040():
     want = dict(ln.split()[::-1] for ln in read("class_tables.sha256").splitlines())
     out = subprocess.run([cli, "--dump-classes"], capture_output=True).stdout
     assert hashlib.sha256(out).hexdigest() == want["class_table_2042040.txt"]
+
+
+# (ctypes mirror in es_sieve.py, the C struct it stands for); field names match
+_LAYOUTS = [
+    (es_sieve.Config, "es_config"),
+    (es_sieve.Counters, "es_counters"),
+    (es_sieve.Record, "es_record"),
+    (es_sieve.Records, "es_records"),
+    (es_sieve.Window, "es_window"),
+    (es_sieve.Info, "es_info_t"),
+    (es_sieve.Schedule, "es_schedule"),
+    (es_sieve.Timing, "es_timing_t"),
+]
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes structure the Python binding passes across the boundary has the size and
+    field offsets of its C declaration (a C program compiled against include/es_sieve.h
+    prints them)."""
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "es_sieve.h"', "int main(void) {"]
+    for cls, cname in _LAYOUTS:
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _t in cls._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", exe], check=True)
+    out = dict(line.rsplit(" ", 1) for line in subprocess.run([exe], capture_output=True, text=True,
+                                                              check=True).stdout.splitlines())
+    for cls, cname in _LAYOUTS:
+        assert int(out["%s size" % cname]) == C.sizeof(cls), cname
+        for fname, _t in cls._fields_:
+            assert int(out["%s.%s" % (cname, fname)]) == getattr(cls, fname).offset, (cname, fname)
