@@ -579,8 +579,9 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
         const WinRef R{wi, x.x, x.y, j};
         // chunks per lane; one chunk is by far the commonest case, so it is tested first.
         const u32 nc = (nmax + 31) >> 5;
-        // four instantiations (1, 2, 4, 8 chunks) measured faster than one per chunk count: the
-        // kernel's code stays small enough for the instruction cache
+        // instantiations for 1, 2 and 4 chunks (8 too when SEG_SMALL is 256) measured faster
+        // than one per chunk count: the kernel's code stays small enough for the instruction
+        // cache
         if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
         else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
         else if constexpr (SEG_SMALL > 128) {
