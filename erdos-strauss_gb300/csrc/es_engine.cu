@@ -716,7 +716,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
     const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tde, T.status, F[w], D[w], rho_slot + w, &slot[w], &B,
-                                                T.rho_budget);
+                                                T.rho_budget, /*use_ecm=*/false);
     if (lane == 0) rung_result(T, s, si, ok, slot[w]);
     __syncwarp();
   }

@@ -218,7 +218,8 @@ constexpr u32 ECM_OWNER_ROUNDS = 32;     // 1024 curves: a 31-bit factor survive
 constexpr u64 ECM_SIGMA_OWNER = 6;       // owner round r: sigma = 6 + 32 r + lane
 
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
-                               int my_k = 0, const HardBoard *board = nullptr, u64 budget = WARP_RHO_STEPS) {
+                               int my_k = 0, const HardBoard *board = nullptr, u64 budget = WARP_RHO_STEPS,
+                               bool use_ecm = true) {
   const Mont M = mont_init(n);
   int slot = -1;                                   // the board slot this warp posted n in
   bool stop = false;                               // cancelled (warp-uniform)
@@ -254,7 +255,7 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
   if (n >= LazyArith::NMAX) {
     f = rho_walk<ExactArith>(n, M, 1 + lane, 32, budget, lane, poll);
   } else {
-    const bool ecm = budget >= ECM_AFTER + ECM_ROUND_STEPS;
+    const bool ecm = use_ecm && budget >= ECM_AFTER + ECM_ROUND_STEPS;
     f = rho_walk<LazyArith>(n, M, 1 + lane, 32, ecm ? ECM_AFTER : budget, lane, poll);
     if (!f && !stop && ecm) {
       u64 steps = ECM_AFTER;
@@ -335,7 +336,8 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
 __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
                                    u32 *status, u32 lane, volatile u64 *rho_slot,
                                    const volatile int *cancel = nullptr, int my_k = 0,
-                                   const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
+                                   const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
+                                   bool use_ecm = true) {
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
   if (n <= 1) return true;
@@ -416,7 +418,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
         const u64 s = isqrt64(v);
         if (s * s == v) { wf_add(F, s, 2, lane); continue; }
-        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board, rho_budget);
+        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board, rho_budget, use_ecm);
         if (d == 0) return false;                  // budget (status set) or cancelled
         if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
         stack[sp++] = d;
@@ -492,10 +494,14 @@ struct RungResult { u64 A; u32 r, k; U128 u; };
 // The rung walk of one prime by one warp, rung after rung (solve_rung3,
 // sieve/rung_scan3.cpp:578-603, in its own order): the throughput form of block_solve_rung
 // below, for while there are more primes than warps. Returns true in every lane when a rung
-// certifies p, with the result in *out (written by lane 0).
+// certifies p, with the result in *out (written by lane 0). use_ecm = false keeps the hard
+// cofactors on rho: with every warp of the GPU busy, a round of curves costs more issue slots
+// than the rho steps it saves (a 10^14-integer window at 10^16, a million primes: 108 ms of
+// stage D with rho alone, 179 ms with ECM), while ECM pays in the latency-bound tail.
 __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac &F,
                                        DPWarp &D, volatile u64 *rho_slot, RungResult *out,
-                                       const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
+                                       const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
+                                       bool use_ecm = true) {
   const u32 lane = threadIdx.x & 31;
   const u32 pm4 = (u32)(p & 3);
   const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
@@ -507,7 +513,7 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board, rho_budget)) return false;
+    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board, rho_budget, use_ecm)) return false;
     const U128 q{p * A, __umul64hi(p, A)};
     const U128 u = warp_min_div_res(p, F, q, r, target, D, lane);
     if (u.lo == 0 && u.hi == 0) continue;
