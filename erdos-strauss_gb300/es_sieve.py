@@ -288,8 +288,9 @@ class Engine:
             sc.long_split = long_split
         self._check(self.lib.es_set_schedule(self.h, C.byref(sc)))
 
-    def autotune(self, windows, repeats=2):
-        """Time the candidate schedules on these windows, keep the fastest; returns it."""
+    def autotune(self, windows, repeats=6):
+        """Time the candidate schedules on these windows (`repeats` timed runs each), keep the
+        one with the lowest mean device time; returns it."""
         n = len(windows)
         w = self.make_windows(windows)
         sc = Schedule()
