@@ -50,7 +50,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_weak_scaling_and_shard_tiling():
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()     # no fork: earlier tests may have left threads
     out = mgr.dict()
     mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
     (i0, t0, m0, sh0, w0), (i1, t1, m1, sh1, w1) = out[0], out[1]
