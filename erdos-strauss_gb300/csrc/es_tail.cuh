@@ -9,8 +9,9 @@
 //   primality        lanes 0..11 each run one of the 12 strong-probable-prime rounds
 //   Brent's rho      all 32 lanes walk with different constants c; the first split wins
 //                    (the factorization is unique, so which lane wins cannot change it)
-//   ECM              a cofactor rho has not split after ECM_AFTER steps gets one elliptic
-//                    curve per lane (es_ecm.cuh), the first divisor wins
+//   ECM              in the latency-bound tail, a cofactor rho has not split after ECM_AFTER
+//                    steps gets rounds of one elliptic curve per lane (es_ecm.cuh), the first
+//                    divisor wins
 //   rung DP          lanes own residue classes t mod r and gather
 //                    nxt[t] = min_j cur[t * pr^-j] * pr^j over j <= e with the bound <= q
 // and a block of four warps walks successive rungs of one prime concurrently, keeping the
