@@ -38,10 +38,11 @@ u64 inv_mod(u64 a, u64 m, bool &ok) {
   return (u64)(t < 0 ? t + (int64_t)m : t);
 }
 
-// A cover candidate tagged with its generation order, so that ties on pmin keep the
-// earliest generated witness -- the replacement rule `pmin < best.pmin` of the reference.
-struct Tagged { Cover c; size_t seq; };
-
+// Cover candidates are collected in full and then reduced to one per (mod, res): the one
+// with the smallest pmin, and among equal pmin the smallest a, then the smallest c. Both
+// generators below reach a given (mod, res, pmin) first through its smallest a, which is the
+// witness the reference keeps (its first-found-wins replacement on pmin), so the rule gives
+// the same (a, c, d) for every cover of the class table.
 static Cover make_cover(u64 a, u64 c, u64 d) {
   const u128 mm = (u128)4 * a * c * d - 1, bb = (u128)4 * a * a * d;
   Cover f;
@@ -52,75 +53,76 @@ static Cover make_cover(u64 a, u64 c, u64 d) {
   return f;
 }
 
-static std::vector<Cover> dedup(std::vector<Tagged> &v) {
-  std::sort(v.begin(), v.end(), [](const Tagged &x, const Tagged &y) {
-    if (x.c.mod != y.c.mod) return x.c.mod < y.c.mod;
-    if (x.c.res != y.c.res) return x.c.res < y.c.res;
-    if (x.c.pmin != y.c.pmin) return x.c.pmin < y.c.pmin;
-    return x.seq < y.seq;
+static std::vector<Cover> dedup(std::vector<Cover> &v) {
+  std::sort(v.begin(), v.end(), [](const Cover &x, const Cover &y) {
+    if (x.mod != y.mod) return x.mod < y.mod;
+    if (x.res != y.res) return x.res < y.res;
+    if (x.pmin != y.pmin) return x.pmin < y.pmin;
+    if (x.a != y.a) return x.a < y.a;
+    return x.c < y.c;
   });
   std::vector<Cover> out;
-  for (const Tagged &t : v)
-    if (out.empty() || out.back().mod != t.c.mod || out.back().res != t.c.res) out.push_back(t.c);
+  for (const Cover &f : v)
+    if (out.empty() || out.back().mod != f.mod || out.back().res != f.res) out.push_back(f);
   return out;
 }
 
 std::vector<Cover> gen_covers(u64 mmax) {
-  std::vector<Tagged> v;
+  std::vector<Cover> v;
   const u64 nmax = (mmax + 1) / 4;
   for (u64 a = 1; a <= nmax; ++a)
     for (u64 d = 1; a * d <= nmax; ++d)
-      for (u64 c = 1; a * d * c <= nmax; ++c) v.push_back({make_cover(a, c, d), v.size()});
+      for (u64 c = 1; a * d * c <= nmax; ++c) v.push_back(make_cover(a, c, d));
   return dedup(v);
 }
 
+// The divisors of n, ascending: each d up to sqrt(n) that divides n pairs with n / d.
+static std::vector<u64> divisors_of(u64 n) {
+  std::vector<u64> lowers, uppers;
+  for (u64 d = 1; d <= n / d; ++d) {
+    if (n % d) continue;
+    lowers.push_back(d);
+    if (d != n / d) uppers.push_back(n / d);
+  }
+  lowers.insert(lowers.end(), uppers.rbegin(), uppers.rend());
+  return lowers;
+}
+
+// Covers whose modulus divides M: an F1 modulus is 4acd - 1, so only the divisors m of M
+// with m = 3 (mod 4) can carry one, and its triples are the ordered factorizations
+// acd = (m + 1) / 4 -- a a divisor of that product, c a divisor of what a leaves.
 std::vector<Cover> gen_wheel_covers(u64 M) {
-  std::vector<u64> divs{1};
-  u64 n = M;
-  for (u64 q = 2; q * q <= n; ++q)
-    if (n % q == 0) {
-      int e = 0;
-      while (n % q == 0) { n /= q; ++e; }
-      const size_t base = divs.size();
-      u64 pe = 1;
-      for (int i = 1; i <= e; ++i) { pe *= q; for (size_t j = 0; j < base; ++j) divs.push_back(divs[j] * pe); }
-    }
-  if (n > 1) { const size_t base = divs.size(); for (size_t j = 0; j < base; ++j) divs.push_back(divs[j] * n); }
-  std::sort(divs.begin(), divs.end());
-  std::vector<Tagged> v;
-  for (u64 m : divs) {
-    if (m % 4 != 3) continue;                 // F1 moduli are 4N - 1
-    const u64 t = (m + 1) / 4;                // acd = t
-    for (u64 a = 1; a <= t; ++a) {
-      if (t % a) continue;
-      const u64 ta = t / a;
-      for (u64 c = 1; c <= ta; ++c)
-        if (ta % c == 0) v.push_back({make_cover(a, c, ta / c), v.size()});
-    }
+  std::vector<Cover> v;
+  for (u64 m : divisors_of(M)) {
+    if (m % 4 != 3) continue;
+    const u64 acd = (m + 1) / 4;
+    for (u64 a : divisors_of(acd))
+      for (u64 c : divisors_of(acd / a)) v.push_back(make_cover(a, c, acd / a / c));
   }
   return dedup(v);
 }
 
+// F2: rung r with the fixed witness u, gcd(r, u) = 1, L = 4ru. For p = rho (mod L) with
+// rho = -r (mod 4), A = (p + r)/4 is determined mod ru and so is q = pA (mod ru): the two
+// conditions of the rung certificate, u | q^2 and q = -u (mod r), hold for every such p or
+// for none, and one evaluation at p = rho decides them. Kept per (L, rho): the smallest
+// (r, u).
 std::vector<Ucert> gen_ucerts(unsigned rmax, unsigned umax) {
   std::vector<Ucert> v;
   for (unsigned r = 1; r <= rmax; ++r)
     for (unsigned u = 1; u <= umax; ++u) {
-      if (gcd_u64(u, r) != 1) continue;
-      const u64 L = 4ull * ((u64)r * u / gcd_u64(r, u));
-      for (u64 rho = 0; rho < L; ++rho) {
-        if ((rho + r) % 4) continue;          // A = (p + r)/4 must be integral
-        bool ok = true;
-        for (int lift = 0; ok && lift < 2; ++lift) {
-          const u64 p = rho + (u64)lift * L, A = (p + r) / 4, q = p * A;
-          if ((q % u) * (q % u) % u || (q + u) % r) ok = false;
-        }
-        if (ok) v.push_back({L, rho, r, u});
+      if (gcd_u64(r, u) != 1) continue;
+      const u64 L = 4ull * r * u;
+      for (u64 rho = (4 - r % 4) % 4; rho < L; rho += 4) {
+        const u64 q = rho * ((rho + r) / 4);
+        const u64 qu = q % u;
+        if (qu * qu % u == 0 && (q + u) % r == 0) v.push_back({L, rho, r, u});
       }
     }
-  // Generation order is (r, u) ascending, so a stable sort on (L, res) followed by keeping
-  // the first of each key keeps the smallest (r, u).
-  std::stable_sort(v.begin(), v.end(), [](const Ucert &x, const Ucert &y) {
-    return x.mod != y.mod ? x.mod < y.mod : x.res < y.res;
+  std::sort(v.begin(), v.end(), [](const Ucert &x, const Ucert &y) {
+    if (x.mod != y.mod) return x.mod < y.mod;
+    if (x.res != y.res) return x.res < y.res;
+    return x.r != y.r ? x.r < y.r : x.u < y.u;
   });
   std::vector<Ucert> out;
   for (const Ucert &c : v)
@@ -128,20 +130,31 @@ std::vector<Ucert> gen_ucerts(unsigned rmax, unsigned umax) {
   return out;
 }
 
+// The class table: a state per residue mod M -- not a unit, a live unit, or a unit some
+// certificate kills. F1 covers with m | M run first (the unit classes they leave are
+// n_f1_only), then the F2 certificates with L | M; a certificate whose modulus does not
+// divide M would kill only part of a class and is skipped.
 Wheel build_wheel(u64 M, const std::vector<Cover> &cov, const std::vector<Ucert> &uc) {
-  std::vector<uint8_t> dead(M, 0);
+  enum : uint8_t { NONUNIT = 0, LIVE = 1, KILLED = 2 };
+  std::vector<uint8_t> state(M);
+  for (u64 x = 0; x < M; ++x) state[x] = gcd_u64(x, M) == 1 ? LIVE : NONUNIT;
+  auto kill = [&](u64 res, u64 mod) {
+    for (u64 x = res; x < M; x += mod)
+      if (state[x] == LIVE) state[x] = KILLED;
+  };
+  auto live = [&]() { return (u64)std::count(state.begin(), state.end(), (uint8_t)LIVE); };
   Wheel w;
-  for (const Cover &f : cov) {
-    if (M % f.mod) continue;
-    w.max_pmin = std::max(w.max_pmin, f.pmin);
-    for (u64 x = f.res; x < M; x += f.mod) dead[x] = 1;
-  }
-  for (u64 x = 1; x < M; ++x) if (!dead[x] && gcd_u64(x, M) == 1) ++w.n_f1_only;
-  for (const Ucert &c : uc) {
-    if (M % c.mod) continue;
-    for (u64 x = c.res; x < M; x += c.mod) dead[x] = 1;
-  }
-  for (u64 x = 1; x < M; ++x) if (!dead[x] && gcd_u64(x, M) == 1) w.classes.push_back(x);
+  for (const Cover &f : cov)
+    if (M % f.mod == 0) {
+      kill(f.res, f.mod);
+      w.max_pmin = std::max(w.max_pmin, f.pmin);
+    }
+  w.n_f1_only = live();
+  for (const Ucert &c : uc)
+    if (M % c.mod == 0) kill(c.res, c.mod);
+  w.classes.reserve(live());
+  for (u64 x = 0; x < M; ++x)
+    if (state[x] == LIVE) w.classes.push_back(x);
   return w;
 }
 
@@ -224,61 +237,67 @@ std::string class_table_text(u64 M) {
   return out;
 }
 
+// Mordell's hard classes mod 840: the residues no polynomial identity of the F1 kind can
+// cover. Every class the derivation keeps must reduce to one of them and be 1 mod 24.
+static bool in_hard_class(u64 c) {
+  static const u64 HARD840[6] = {1, 121, 169, 289, 361, 529};
+  if (c % 24 != 1) return false;
+  for (u64 h : HARD840) if (c % 840 == h) return true;
+  return false;
+}
+
 int wheel_self_test(std::string &log) {
-  int fails = 0;
-  char line[160];
-  auto check = [&](const char *what, u64 got, u64 want) {
-    if (got != want) { snprintf(line, sizeof line, "  FAIL %-34s got %llu want %llu\n", what, got, want); ++fails; }
-    else snprintf(line, sizeof line, "  ok   %-34s %llu\n", what, got);
-    log += line;
-  };
+  struct Row { std::string what; u64 got, want; };
+  std::vector<Row> rows;
+  auto fnv_text = [](u64 h) { char b[24]; snprintf(b, sizeof b, "%016llx", h); return std::string(b); };
+  // 1. The divisor-driven generator against the full enumeration, restricted to m | M, at the
+  //    largest modulus where the full enumeration is cheap.
   {
-    std::vector<Cover> slow;
-    for (const Cover &f : gen_covers(120120)) if (120120 % f.mod == 0) slow.push_back(f);
-    const std::vector<Cover> fast = gen_wheel_covers(120120);
-    u64 diff = slow.size() != fast.size();
-    for (size_t i = 0; !diff && i < slow.size(); ++i)
-      diff = !(slow[i].mod == fast[i].mod && slow[i].res == fast[i].res && slow[i].pmin == fast[i].pmin &&
-               slow[i].a == fast[i].a && slow[i].c == fast[i].c && slow[i].d == fast[i].d);
-    check("wheel covers: divisor == full", diff, 0);
-    check("wheel covers at 120120", fast.size(), slow.size());
+    std::vector<Cover> full;
+    for (const Cover &f : gen_covers(120120)) if (120120 % f.mod == 0) full.push_back(f);
+    const std::vector<Cover> divd = gen_wheel_covers(120120);
+    u64 mismatches = full.size() == divd.size() ? 0 : 1;
+    for (size_t i = 0; !mismatches && i < full.size(); ++i)
+      mismatches += full[i].mod != divd[i].mod || full[i].res != divd[i].res || full[i].pmin != divd[i].pmin ||
+                    full[i].a != divd[i].a || full[i].c != divd[i].c || full[i].d != divd[i].d;
+    rows.push_back({"120120: divisor covers differing from full", mismatches, 0});
+    rows.push_back({"120120: covers with m | M", divd.size(), full.size()});
   }
   const std::vector<Ucert> uc = gen_ucerts(UCERT_RMAX, UCERT_UMAX);
+  // 2. M = 840: the derivation must land on exactly Mordell's six hard classes.
   const Wheel w840 = build_wheel(840, gen_covers(840), uc);
-  check("wheel(840) F1 only", w840.n_f1_only, 24);
-  check("wheel(840) classes", w840.classes.size(), 6);
-  check("wheel(840) max pmin", w840.max_pmin, 34);
-  static const u64 REF840[6] = {1, 121, 169, 289, 361, 529};
-  bool same = w840.classes.size() == 6;
-  for (int i = 0; same && i < 6; ++i) same = w840.classes[i] == REF840[i];
-  log += same ? "  ok   wheel(840) == hard classes (DERIVED, not assumed)\n"
-              : "  FAIL wheel(840) != {1,121,169,289,361,529}\n";
-  if (!same) ++fails;
+  rows.push_back({"840: units left by F1", w840.n_f1_only, 24});
+  rows.push_back({"840: classes left by F1+F2", w840.classes.size(), 6});
+  rows.push_back({"840: largest pmin of a wheel cover", w840.max_pmin, 34});
+  u64 off840 = w840.classes.size() == 6 ? 0 : 1;
+  for (u64 c : w840.classes) off840 += !in_hard_class(c);
+  rows.push_back({"840: classes that are not hard classes", off840, 0});
+  // 3. M = 120120 (full enumeration) and M = 2042040 (divisor covers): counts and pins.
   const Wheel w120 = build_wheel(120120, gen_covers(120120), uc);
-  check("wheel(120120) F1 only", w120.n_f1_only, 920);
-  check("wheel(120120) classes", w120.classes.size(), 220);
-  check("wheel(120120) max pmin", w120.max_pmin, 15014);
-  const u64 h = fnv64_classes(w120.classes);
-  if (h != class_pin(120120)->fnv64) { snprintf(line, sizeof line, "  FAIL wheel(120120) fnv64 %016llx want dbc4ab9b16d73f76\n", h); ++fails; }
-  else snprintf(line, sizeof line, "  ok   wheel(120120) fnv64            dbc4ab9b16d73f76\n");
-  log += line;
+  rows.push_back({"120120: units left by F1", w120.n_f1_only, 920});
+  rows.push_back({"120120: classes left by F1+F2", w120.classes.size(), 220});
+  rows.push_back({"120120: largest pmin of a wheel cover", w120.max_pmin, 15014});
+  rows.push_back({"120120: fnv64 " + fnv_text(fnv64_classes(w120.classes)) + " differs from the pin",
+                  fnv64_classes(w120.classes) != class_pin(120120)->fnv64, 0});
   const Wheel w204 = build_wheel(2042040, gen_wheel_covers(2042040), uc);
-  check("wheel(2042040) classes", w204.classes.size(), 2308);
-  const u64 h2 = fnv64_classes(w204.classes);
-  if (h2 != class_pin(2042040)->fnv64) { snprintf(line, sizeof line, "  FAIL wheel(2042040) fnv64 %016llx want %016llx\n", h2, class_pin(2042040)->fnv64); ++fails; }
-  else snprintf(line, sizeof line, "  ok   wheel(2042040) fnv64           %016llx\n", h2);
-  log += line;
-  auto strays_of = [&](const Wheel &w) {
-    u64 strays = 0;
-    for (u64 c : w.classes) {
-      bool hard = false;
-      for (u64 hc : REF840) if (c % 840 == hc) hard = true;
-      if (c % 24 != 1 || !hard) ++strays;
-    }
-    return strays;
-  };
-  check("wheel(2042040) outside hard class", strays_of(w204), 0);
-  check("survivors outside hard class", strays_of(w120), 0);
+  rows.push_back({"2042040: classes left by F1+F2", w204.classes.size(), 2308});
+  rows.push_back({"2042040: fnv64 " + fnv_text(fnv64_classes(w204.classes)) + " differs from the pin",
+                  fnv64_classes(w204.classes) != class_pin(2042040)->fnv64, 0});
+  // 4. Both larger tables reproduce Mordell: nothing outside the hard classes survives.
+  for (const auto &mw : {std::make_pair("120120", &w120), std::make_pair("2042040", &w204)}) {
+    u64 off = 0;
+    for (u64 c : mw.second->classes) off += !in_hard_class(c);
+    rows.push_back({std::string(mw.first) + ": classes outside the hard classes", off, 0});
+  }
+  int fails = 0;
+  char line[200];
+  for (const Row &r : rows) {
+    const bool ok = r.got == r.want;
+    fails += !ok;
+    if (ok) snprintf(line, sizeof line, "  pass  %-50s = %llu\n", r.what.c_str(), r.got);
+    else snprintf(line, sizeof line, "  FAIL  %-50s = %llu, expected %llu\n", r.what.c_str(), r.got, r.want);
+    log += line;
+  }
   return fails;
 }
 

@@ -43,8 +43,10 @@ u64 inv_mod(u64 a, u64 m, bool &ok);                      // extended Euclid (in
 
 // The class table artifact (--dump-classes, sieve/rung_scan3.cpp:904-953), as text.
 std::string class_table_text(u64 M);
-// The --verify self-test constants (sieve/rung_scan3.cpp:821-897); prints ok/FAIL lines
-// into `log` and returns the failure count.
+// The --verify self-test: the same constants as sieve/rung_scan3.cpp:821-897 checks (the
+// divisor-driven covers against the full enumeration, the 840 / 120120 / 2042040 tables and
+// their pins, Mordell's hard classes); one pass/FAIL line per check into `log`; returns the
+// failure count.
 int wheel_self_test(std::string &log);
 
 }  // namespace es

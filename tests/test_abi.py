@@ -164,3 +164,15 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert int(out["%s size" % cname]) == C.sizeof(cls), cname
         for fname, _t in cls._fields_:
             assert int(out["%s.%s" % (cname, fname)]) == getattr(cls, fname).offset, (cname, fname)
+
+
+def test_cli_self_test_wheel_checks_pass_on_the_host():
+    """--verify's host checks (the class-table derivation against the constants of
+    sieve/rung_scan3.cpp:821-897) pass without a GPU; only the device line needs one."""
+    cli = es_sieve.CLI_PATH
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    out = subprocess.run([cli, "--verify"], capture_output=True, text=True).stdout
+    host = [ln for ln in out.splitlines() if ln.startswith("  ") and "device" not in ln]
+    assert len(host) == 14
+    assert all(ln.startswith("  pass ") for ln in host), out
