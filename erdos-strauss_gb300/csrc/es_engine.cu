@@ -907,6 +907,7 @@ struct Request {
   es_status st = ES_OK;
   std::string err;
   bool done = false;
+  bool claimed = false;                 // an es_poll is waiting on it (one poller per ticket)
   u64 mem = 0;                          // admitted device-memory estimate
 };
 }  // namespace es
@@ -952,6 +953,7 @@ struct es_engine {
   uint64_t next_ticket = 1;
   es::u64 mem_in_use = 0;
   size_t queued_windows = 0;
+  int pollers = 0;                      // es_poll calls inside the engine (es_close waits for them)
   std::vector<std::thread> workers;
   bool stopping = false;
 };
@@ -1606,18 +1608,22 @@ static es_status build_tables(es_engine *e) {
   temps.p[2] = d_g;
   CU(cudaMalloc(&d_inv, std::max<size_t>(nf, 1) * sizeof(u32)));
   temps.p[3] = d_inv;
-  CU(cudaMemcpy(e->d_rho, rho.data(), L * sizeof(u32), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(e->d_fdesc, fdesc.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(e->d_sdist, sd.data(), sd.size() * sizeof(u32), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(e->d_tdp, tdp.data(), tdp.size() * sizeof(u32), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(e->d_tde, tde.data(), tde.size() * sizeof(TdEntry), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(d_mods, om.data(), nf * sizeof(u64), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(d_ress, orr.data(), nf * sizeof(u64), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(d_inv, oinv.data(), nf * sizeof(u32), cudaMemcpyHostToDevice));
+  // The table copies go on the stream the build kernels run on (slot 0's, non-blocking, so not
+  // ordered after the legacy stream); the host vectors they read outlive the synchronisation
+  // at the end of this function.
+  cudaStream_t bs = e->slots[0].stream;
+  CU(cudaMemcpyAsync(e->d_rho, rho.data(), L * sizeof(u32), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(e->d_fdesc, fdesc.data(), nf * sizeof(u32), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(e->d_sdist, sd.data(), sd.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(e->d_tdp, tdp.data(), tdp.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(e->d_tde, tde.data(), tde.size() * sizeof(TdEntry), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(d_mods, om.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(d_ress, orr.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice, bs));
+  CU(cudaMemcpyAsync(d_inv, oinv.data(), nf * sizeof(u32), cudaMemcpyHostToDevice, bs));
   const u64 total = (u64)L * e->ldk;
-  k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
-                                                                       e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
+  k_build_k0<<<(unsigned)((total + 255) / 256), 256, 0, bs>>>(e->d_rho, L, d_mods, d_ress, d_g, d_inv,
+                                                              e->d_fdesc, (u32)nf, e->ldk, e->d_K0);
   CU(cudaGetLastError());
   // Kill masks for short windows: within each phase (covers, then stage-B' primes), the
   // smallest strides get a mask while the per-lane table fits MASK_BYTES_MAX; the filters of
@@ -1682,17 +1688,17 @@ static es_status build_tables(es_engine *e) {
     CU(cudaMalloc(&e->d_lfil, std::max<size_t>(lfil.size(), 1) * sizeof(u32)));
     CU(cudaMalloc(&d_fmask, std::max<size_t>(nf, 1) * sizeof(int)));
     temps.p[4] = d_fmask;
-    CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), e->slots[0].stream));
-    if (!md.empty()) CU(cudaMemcpy(e->d_mdesc, md.data(), md.size() * sizeof(MaskDesc), cudaMemcpyHostToDevice));
-    if (!lfil.empty()) CU(cudaMemcpy(e->d_lfil, lfil.data(), lfil.size() * sizeof(u32), cudaMemcpyHostToDevice));
-    if (nf) CU(cudaMemcpy(d_fmask, fmask.data(), nf * sizeof(int), cudaMemcpyHostToDevice));
+    CU(cudaMemsetAsync(e->d_mtab, 0, (size_t)L * e->Wpad * sizeof(u64), bs));
+    if (!md.empty()) CU(cudaMemcpyAsync(e->d_mdesc, md.data(), md.size() * sizeof(MaskDesc), cudaMemcpyHostToDevice, bs));
+    if (!lfil.empty()) CU(cudaMemcpyAsync(e->d_lfil, lfil.data(), lfil.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
+    if (nf) CU(cudaMemcpyAsync(d_fmask, fmask.data(), nf * sizeof(int), cudaMemcpyHostToDevice, bs));
     if (nf && !md.empty()) {
       const u64 tt = (u64)L * nf;
       k_build_masks<<<(unsigned)((tt + 255) / 256), 256, 0, e->slots[0].stream>>>(e->d_K0, L, e->ldk, (u32)nf, d_fmask,
                                                                          e->d_mdesc, e->Wpad, e->d_mtab);
       CU(cudaGetLastError());
     }
-    CU(cudaStreamSynchronize(e->slots[0].stream));
+    CU(cudaStreamSynchronize(bs));
     CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc))));
   }
@@ -1805,17 +1811,21 @@ static es_status probe(es_engine *e, Slot *sl, size_t count, size_t in_bytes, co
   (void)out_bytes;
   CU(cudaMalloc(&d_in, std::max<size_t>(in_bytes, 8)));
   for (size_t i = 0; i < outs.size(); ++i) CU(cudaMalloc(&d_outs[i], std::max<size_t>(outs[i].second, 8)));
-  CU(cudaMemcpy(d_in, in, in_bytes, cudaMemcpyHostToDevice));
+  // Every copy is queued on the probe's own stream (a non-blocking stream is not ordered after
+  // the legacy stream that a plain cudaMemcpy uses), and the host waits for that stream before
+  // it reads anything back.
+  CU(cudaMemcpyAsync(d_in, in, in_bytes, cudaMemcpyHostToDevice, sl->stream));
   CU(cudaMemsetAsync(sl->d_status, 0, sizeof(u32), sl->stream));
   CU(cudaEventRecord(sl->ev[9], sl->stream));
   launch(d_in, d_outs);
   CU(cudaGetLastError());
   CU(cudaEventRecord(sl->ev[10], sl->stream));
+  for (size_t i = 0; i < outs.size(); ++i)
+    CU(cudaMemcpyAsync(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost, sl->stream));
+  u32 st = 0;
+  CU(cudaMemcpyAsync(&st, sl->d_status, sizeof st, cudaMemcpyDeviceToHost, sl->stream));
   CU(cudaStreamSynchronize(sl->stream));
   sl->timing.total_ms = ev_ms(sl->ev[9], sl->ev[10]);   // the probe kernel alone
-  for (size_t i = 0; i < outs.size(); ++i) CU(cudaMemcpy(outs[i].first, d_outs[i], outs[i].second, cudaMemcpyDeviceToHost));
-  u32 st = 0;
-  CU(cudaMemcpy(&st, sl->d_status, sizeof st, cudaMemcpyDeviceToHost));
   (void)count;
   if (st) return fail(e, ES_ERR_DEVICE_STATUS, "device status:" + status_text(st));
   return ES_OK;
@@ -1913,10 +1923,11 @@ es_status es_open(const es_config *cfg, es_engine **out) {
   e->filter_fnv = fnv64_filters(e->mods, e->ress, e->ncov);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= e->device || e->device < 0) {
+    g_open_error = "no CUDA device " + std::to_string(e->device);
     delete e;
     return ES_ERR_CUDA;
   }
-  if (cudaSetDevice(e->device) != cudaSuccess) { delete e; return ES_ERR_CUDA; }
+  if (cudaSetDevice(e->device) != cudaSuccess) { g_open_error = "cudaSetDevice failed"; delete e; return ES_ERR_CUDA; }
   cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, e->device);
   for (Slot &sl : e->slots) {
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1951,6 +1962,13 @@ es_status es_close(es_engine *e) {
   }
   e->qcv.notify_all();
   for (std::thread &t : e->workers) t.join();
+  {
+    // the workers finished every queued request; a poller still inside es_poll has been woken
+    // and owns its request until it returns
+    std::unique_lock<std::mutex> lk(e->qmu);
+    e->dcv.notify_all();
+    e->dcv.wait(lk, [&] { return e->pollers == 0; });
+  }
   for (auto &kv : e->reqs) delete kv.second;
   cudaSetDevice(e->device);
   for (Slot &sl : e->slots) {
@@ -2269,10 +2287,22 @@ es_status es_poll(es_engine *e, uint64_t ticket, es_counters *per_window, es_rec
   auto it = e->reqs.find(ticket);
   if (it == e->reqs.end()) return fail(e, ES_ERR_ARG, "unknown ticket");
   Request *r = it->second;
+  // One poller per ticket: a second one would read the request while the first deletes it.
+  if (r->claimed) return fail(e, ES_ERR_ARG, "ticket is already being polled");
+  r->claimed = true;
+  ++e->pollers;
   auto ready = [&] { return r->done; };
+  bool done = true;
   if (timeout_ms < 0) e->dcv.wait(lk, ready);
-  else if (!e->dcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return ES_ERR_TIMEOUT;
-  e->reqs.erase(it);
+  else done = e->dcv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
+  --e->pollers;
+  if (!done) {
+    r->claimed = false;                  // the ticket stays valid; the caller may poll again
+    e->dcv.notify_all();
+    return ES_ERR_TIMEOUT;
+  }
+  e->reqs.erase(r->ticket);
+  e->dcv.notify_all();                   // es_close may be waiting for the last poller
   lk.unlock();
   const es_status st = r->st;
   if (st == ES_OK) {

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <unordered_map>
 
 namespace es {
 
@@ -49,21 +50,41 @@ __global__ void k_noalloc_round2(const u64 *__restrict__ n, unsigned char *__res
   }
 }
 
-// The device address of the scratch array, looked up once per device with that device
-// current. In host code g_noalloc_scratch names a host-side stand-in, never the device array.
+// The device address of the scratch array, looked up once per CUDA context with that
+// context current (in host code g_noalloc_scratch names a host-side stand-in, never the device
+// array). The cache is keyed by the driver's context id, which no later context reuses: after a
+// cudaDeviceReset the device's new primary context gets a new id, so the address is looked up
+// again in the new context instead of pointing into the destroyed one.
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
 static std::mutex g_noalloc_mu;
-static u32 *g_noalloc_ptr[64];
+static std::unordered_map<unsigned long long, u32 *> g_noalloc_ptr;
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+static CtxGetIdFn g_ctx_get_id = nullptr;
 
-static cudaError_t noalloc_scratch(int dev, u32 **out) {
+static cudaError_t noalloc_scratch(u32 **out) {
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorNotSupported;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != 0 || !ctx || g_ctx_get_id(ctx, &id) != 0) return cudaErrorDeviceUninitialized;
+  auto it = g_noalloc_ptr.find(id);
+  if (it == g_noalloc_ptr.end()) {
     void *p = nullptr;
     const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess) return err;
-    g_noalloc_ptr[dev] = static_cast<u32 *>(p);
+    it = g_noalloc_ptr.emplace(id, static_cast<u32 *>(p)).first;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = it->second;
   return cudaSuccess;
 }
 
@@ -76,8 +97,10 @@ extern "C" es_status es_is_prime_noalloc(const uint64_t *d_n, size_t count, uint
   if (count > ES_NOALLOC_MAX) return ES_ERR_ARG;     // the scratch list holds ES_NOALLOC_MAX indices
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return ES_ERR_CUDA;
+  // makes the device's primary context current on this thread (it allocates nothing)
+  if (cudaSetDevice(dev) != cudaSuccess) return ES_ERR_CUDA;
   u32 *scratch = nullptr;
-  if (noalloc_scratch(dev, &scratch) != cudaSuccess) return ES_ERR_CUDA;
+  if (noalloc_scratch(&scratch) != cudaSuccess) return ES_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ES_ERR_CUDA;

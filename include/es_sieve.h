@@ -168,8 +168,10 @@ es_status es_run_batch(es_engine *engine, const es_window *w, size_t n, int sche
  * es_open); ES_ERR_RANGE at once for a window the run would refuse. es_poll waits up to
  * timeout_ms (negative: without limit; 0: just checks) and returns ES_ERR_TIMEOUT if the
  * request is not done; otherwise it fills per_window (one entry per submitted window) and
- * recs (window indices relative to the request) and forgets the ticket. No reference
- * counterpart. */
+ * recs (window indices relative to the request) and forgets the ticket. A ticket has one
+ * poller at a time: a second es_poll on a ticket that is being waited on returns ES_ERR_ARG.
+ * es_close waits for es_poll calls already inside the engine; no call may start on an engine
+ * after es_close has begun. No reference counterpart. */
 es_status es_submit(es_engine *engine, const es_window *w, size_t n, uint64_t *ticket);
 es_status es_poll(es_engine *engine, uint64_t ticket, es_counters *per_window, es_records *recs,
                   int timeout_ms);
@@ -254,9 +256,10 @@ size_t es_sha256_hex(const void *data, size_t n, char *out, size_t cap);
  * Its scratch is a fixed array of (ES_NOALLOC_MAX + 64) 32-bit words in the library's
  * device image, held by every GPU that loads the library until the process exits; the call
  * itself allocates nothing. count above ES_NOALLOC_MAX is refused with ES_ERR_ARG. The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress), so make it
- * before any stream capture. Every call shares the one array: calls that overlap on the GPU
- * (on different streams, or from different threads) race; serialise them. */
+ * call in a CUDA context (the device's primary context, and again after a cudaDeviceReset has
+ * replaced it) looks up the array's device address (cudaGetSymbolAddress), so make it before
+ * any stream capture. Every call shares the one array: calls that overlap on the GPU (on
+ * different streams, or from different threads) race; serialise them. */
 #define ES_NOALLOC_MAX (1u << 20)
 es_status es_is_prime_noalloc(const uint64_t *d_n, size_t count, uint8_t *d_out, void *stream);
 

@@ -105,6 +105,13 @@ int es_o_sprp2(u64 n) {
   return 0;
 }
 
+/* The scan's primality verdict (sprp2 && is_prime, sieve/rung_scan3.cpp:686-689) over an
+ * array, threads over values: out[i] = 1 for a prime. */
+void es_o_is_prime_batch(const u64 *n, size_t count, uint8_t *out) {
+  #pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < count; ++i) out[i] = (uint8_t)(es_o_sprp2(n[i]) && es_o_is_prime(n[i]));
+}
+
 /* ------------------------------------------------------------ factorization
  * The factorization of n is unique, so any exact method gives the certificate the
  * reference gives: min_div_res takes a minimum over divisors and divisors3 sorts

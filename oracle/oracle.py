@@ -29,6 +29,7 @@ def lib():
         u64, P = C.c_uint64, C.POINTER
         L.es_o_is_prime.argtypes = [u64]; L.es_o_is_prime.restype = C.c_int
         L.es_o_sprp2.argtypes = [u64]; L.es_o_sprp2.restype = C.c_int
+        L.es_o_is_prime_batch.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]; L.es_o_is_prime_batch.restype = None
         L.es_o_factor.argtypes = [u64, P(u64), P(C.c_int)]; L.es_o_factor.restype = C.c_int
         L.es_o_solve_rung.argtypes = [u64, C.c_char_p, C.c_size_t]; L.es_o_solve_rung.restype = C.c_int
         L.es_o_solve_direct.argtypes = [u64, C.c_char_p, C.c_size_t]; L.es_o_solve_direct.restype = C.c_int
@@ -44,6 +45,15 @@ def lib():
 
 def is_prime(n):
     return bool(lib().es_o_sprp2(n) and lib().es_o_is_prime(n))
+
+
+def is_prime_array(values):
+    """Verdicts for a numpy uint64 array (threads over values): a uint8 array, 1 = prime."""
+    import numpy as np
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    out = np.zeros(len(v), dtype=np.uint8)
+    lib().es_o_is_prime_batch(v.ctypes.data, len(v), out.ctypes.data)
+    return out
 
 
 def factor(n):
