@@ -16,7 +16,10 @@
 //                      (sieve/cuda/scan.cu:266-310: rounds of --seg positions, lanes in wheel
 //                      order within a round), running the shard in chunks of R rounds (default
 //                      64) so no chunk holds more than its own records; --order lane emits
-//                      rung_scan3's order and runs the shard as one window. And
+//                      rung_scan3's order and runs the shard as one window.
+//   --order round|lane without --meta: the stdout stream in that order (default lane, the
+//                      order of rung_scan3; round is the production driver's, whose streams the
+//                      published window digests are taken over). And
 //   rung_scan3_gb300 --batch FILE [flags]   one "LO HI" per line, each window's stream and
 //                                           SUMMARY in file order, run as one batch;
 //   rung_scan3_gb300 --serve FILE|- [flags] the same lines read as they arrive (stdin for
@@ -233,13 +236,13 @@ static int self_test(int device) {
   fputs(log.c_str(), stdout);
   // The device path: primality of known values, and one rung certificate.
   es_engine *e = default_engine(device);
-  if (!e) { printf("  FAIL device engine\n"); ++fails; }
+  if (!e) { printf("  FAIL  device engine could not be opened\n"); ++fails; }
   else {
     const u64 v[6] = {2, 3037000493ull, 4611686018427387847ull, 18446744073709551557ull, 561, 3215031751ull};
     const uint8_t want[6] = {1, 1, 1, 1, 0, 0};
     uint8_t got[6] = {0};
     const bool ok = es_is_prime_batch(e, v, 6, got) == ES_OK && !memcmp(got, want, 6);
-    printf(ok ? "  ok   device Miller-Rabin                 6\n" : "  FAIL device Miller-Rabin\n");
+    printf(ok ? "  pass  %-50s = 6\n" : "  FAIL  %-50s\n", "device Miller-Rabin verdicts on known values");
     if (!ok) ++fails;
     es_close(e);
   }
@@ -265,6 +268,18 @@ static std::string file_sha256(const char *path) {
 // next, and a stable counting sort of a chunk's lane-major records by J / seg gives round,
 // lane, J. A producer thread keeps the GPU on the next chunk while this one is sorted,
 // formatted by several threads and hashed in order.
+// Records of one window (lane-major: lane, then J) put in the production driver's round-major
+// order (round J / seg, then lane, then J) by a stable counting sort on the round.
+static void sort_round_major(const es_record *rec, size_t n, u64 seg, std::vector<es_record> &out) {
+  u64 rmax = 0;
+  for (size_t i = 0; i < n; ++i) rmax = std::max<u64>(rmax, rec[i].J / seg);
+  std::vector<size_t> start(rmax + 2, 0);
+  for (size_t i = 0; i < n; ++i) ++start[rec[i].J / seg + 1];
+  for (size_t k = 1; k < start.size(); ++k) start[k] += start[k - 1];
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) out[start[rec[i].J / seg]++] = rec[i];
+}
+
 struct Chunk {
   es_counters c{};
   es_records r{nullptr, 0};
@@ -327,14 +342,8 @@ static int write_meta(es_engine *e, const char *path, u64 lo, u64 hi, u64 M, u64
     tot.composite += c.composite; tot.rung += c.rung; tot.direct += c.direct; tot.survivors += c.survivors;
     const es_record *rec = ch.r.recs;
     const size_t n = ch.r.n;
-    if (round_order && n) {                            // stable counting sort by round
-      u64 rmax = 0;
-      for (size_t i = 0; i < n; ++i) rmax = std::max<u64>(rmax, rec[i].J / seg);
-      std::vector<size_t> start(rmax + 2, 0);
-      for (size_t i = 0; i < n; ++i) ++start[rec[i].J / seg + 1];
-      for (size_t k = 1; k < start.size(); ++k) start[k] += start[k - 1];
-      sorted.resize(n);
-      for (size_t i = 0; i < n; ++i) sorted[start[rec[i].J / seg]++] = rec[i];
+    if (round_order && n) {
+      sort_round_major(rec, n, seg, sorted);
       rec = sorted.data();
     }
     std::vector<std::thread> pool;
@@ -427,7 +436,7 @@ int main(int argc, char **argv) {
   u64 lo = 0, hi = 0;
   if (!batch && !serve) { lo = strtoull(argv[1], 0, 10); hi = strtoull(argv[2], 0, 10); }
   u64 M = 2042040, mmax = 10000, seg = 262144, shard = 0, nshard = 1, sieve_p = 0;
-  bool emit_surv = true, profile = false, no_rung = false, autotune = false, round_order = true;
+  bool emit_surv = true, profile = false, no_rung = false, autotune = false, round_order = true, order_given = false;
   const char *ffile = nullptr, *meta = nullptr, *threads = "1";
   u64 chunk_rounds = 64;
   for (int i = 3; i < argc; ++i) {
@@ -450,6 +459,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(argv[i], "--chunk-rounds") && i + 1 < argc) chunk_rounds = strtoull(argv[++i], 0, 10);
     else if (!strcmp(argv[i], "--order") && i + 1 < argc) {
       const char *o = argv[++i];
+      order_given = true;
       if (!strcmp(o, "round")) round_order = true;
       else if (!strcmp(o, "lane")) round_order = false;
       else { fprintf(stderr, "FATAL: --order must be round or lane\n"); return 1; }
@@ -560,10 +570,16 @@ int main(int argc, char **argv) {
   const auto t2 = std::chrono::steady_clock::now();
   u64 survivors = 0;
   size_t r0 = 0;
+  std::vector<es_record> sorted;
   for (size_t w = 0; w < wins.size(); ++w) {
     size_t r1 = r0;
     while (r1 < recs.n && recs.recs[r1].window == w) ++r1;
-    print_records(stdout, recs.recs + r0, r1 - r0, emit_surv);
+    if (order_given && round_order) {              // the production driver's round-major order
+      sort_round_major(recs.recs + r0, r1 - r0, seg, sorted);
+      print_records(stdout, sorted.data(), sorted.size(), emit_surv);
+    } else {
+      print_records(stdout, recs.recs + r0, r1 - r0, emit_surv);
+    }
     char line[512];
     fputs(es_format_summary(e, wins[w].lo, wins[w].hi, &cnt[w], line, sizeof line) ? line : "SUMMARY ?\n", stdout);
     survivors += cnt[w].survivors;

@@ -9,6 +9,8 @@ stand in for its configurations with the same shapes, sizes and distributions:
   batch  4096 windows, lengths floor(2^(16 + 12 U1)), starts
          floor(exp(ln 255255 + U2 (ln 1.8446744065e19 - ln 255255))), clamped into
          [255255, DIRECT_PMAX - len]
+  batch19  the same length law, starts log-uniform over [10^19, DIRECT_PMAX - len]: the
+         batched configuration at the height the run19/run64 shards cover
   serve  Poisson arrivals (mean gap 0.5 ms), lengths log-uniform in [2^12, 2^30], starts as
          for the batch
 """
@@ -19,6 +21,7 @@ SEED = 0xE52026
 DIRECT_PMAX = 18446744065119614976        # (2^32-1)^2 - 2048 - 1
 FLOOR_2042040 = 255254                    # wheel_pmin of the 2042040 table
 TOP = 18446744065000000000                # 1.8446744065e19, the batch's upper height
+BASE19 = 10 ** 19                         # lowest start of the batch at the top of the range
 
 
 class SplitMix64:
@@ -72,6 +75,31 @@ def batch_windows(n=4096, seed=SEED, lmin_log2=16, lmax_log2=28, lo_min=FLOOR_20
         lo = max(lo, lo_min)
         lo = min(lo, DIRECT_PMAX - length)
         out.append((lo, lo + length))
+    return out
+
+
+def batch19_windows(n=4096, seed=SEED, lmin_log2=16, lmax_log2=28):
+    """The batched configuration at the top of the range: the same length law as
+    batch_windows, starts log-uniform over [10^19, DIRECT_PMAX - len]."""
+    g = SplitMix64(seed ^ 0x19)
+    out = []
+    for _ in range(n):
+        length = int(2.0 ** (lmin_log2 + (lmax_log2 - lmin_log2) * g.uniform()))
+        top = DIRECT_PMAX - length
+        lo = min(max(_height(g, BASE19, top), BASE19), top)
+        out.append((lo, lo + length))
+    return out
+
+
+def read_windows(path):
+    """Windows from a file of "LO HI" lines (the committed fixtures keep the exact windows,
+    so that a platform whose libm rounds exp or log differently still runs the same ones)."""
+    out = []
+    with open(path) as f:
+        for ln in f:
+            t = ln.split()
+            if len(t) == 2:
+                out.append((int(t[0]), int(t[1])))
     return out
 
 

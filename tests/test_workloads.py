@@ -39,3 +39,21 @@ def test_c3_window():
     c = workloads.c3()
     assert c["hi"] - c["lo"] == 2 ** 34 and c["lo"] >= 17 * 10 ** 18 and c["hi"] <= workloads.DIRECT_PMAX
     assert c == workloads.c3()
+
+
+def test_batch19_windows_shape():
+    w = workloads.batch19_windows(4096)
+    assert w == workloads.batch19_windows(4096) and len(w) == 4096
+    lens = [hi - lo for lo, hi in w]
+    assert min(lens) >= 2 ** 16 and max(lens) < 2 ** 28
+    assert all(lo >= 10 ** 19 and hi <= workloads.DIRECT_PMAX for lo, hi in w)
+    assert abs(statistics.mean(math.log2(x) for x in lens) - 22) < 0.3
+    assert 1.1e11 < sum(lens) < 1.6e11
+
+
+def test_committed_batch_windows_are_the_seeded_ones():
+    """The fixtures keep the exact windows; on this host workloads.py draws the same ones."""
+    import os
+    gen = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gen")
+    assert workloads.read_windows(os.path.join(gen, "batch4096.windows")) == workloads.batch_windows(4096)
+    assert workloads.read_windows(os.path.join(gen, "batch19_4096.windows")) == workloads.batch19_windows(4096)
