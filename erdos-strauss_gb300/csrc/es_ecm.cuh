@@ -118,13 +118,19 @@ __device__ __forceinline__ u64 proper_gcd(u64 g, u64 n) {
   return (d > 1 && d < n) ? d : 0;
 }
 
-// Giant steps between polls in stage 2.
+// Giant steps between polls in stage 2, ladder bits between polls in stage 1 (a poll that
+// answers "stop" ends the curve at once: another walk or curve has split the cofactor).
 constexpr int ECM_STAGE2_POLL = 24;
+#ifndef ES_ECM_STAGE1_POLL
+#define ES_ECM_STAGE1_POLL 13
+#endif
+constexpr int ECM_STAGE1_POLL = ES_ECM_STAGE1_POLL;
 
 // One ECM curve (Suyama's sigma, 6 <= sigma < n) on the odd composite n > 2^32, in the
 // arithmetic Ar (LazyArith needs n < 2^62). Returns a proper divisor of n, or 0 when this curve
-// found none. poll() is called at the same points in every lane (after stage 1 and every
-// ECM_STAGE2_POLL giant steps); when it returns true the curve stops early and returns 0. dead
+// found none. poll() is called at the same points in every lane (every ECM_STAGE1_POLL ladder
+// bits, after stage 1 and every ECM_STAGE2_POLL giant steps); when it returns true the curve
+// stops early and returns 0. dead
 // lanes keep computing (their result is dropped) so that the lanes of a warp stay in step.
 template <class Ar, class Poll>
 __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
@@ -160,6 +166,7 @@ __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
     R1 = ecm_add1<Ar>(R0, R1, x, M);
     R0 = ecm_dbl<Ar>(R0, a24, M);
     if (b) { const XZ t = R0; R0 = R1; R1 = t; }
+    if (i && i % ECM_STAGE1_POLL == 0 && poll()) return 0;
   }
   const XZ Q = R0;
   if (!dead) {

@@ -309,25 +309,26 @@ __device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFF
 template <int NC>
 __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], const u32 (&b)[SHORT_LANES],
                                                  const u32 *tab, u32 tab_words, const MaskDesc *smd, u32 m0,
-                                                 u32 m1, const u16 *__restrict__ Qrow, u32 q0_first, u32 lane) {
+                                                 u32 m1, const u16 *__restrict__ Qrow, u32 q0_first, u32 lane,
+                                                 const MaskDesc &md_first) {
   u32 kill[SHORT_LANES][NC];
   // Round one (strides m0 .. m0 + 31, q0_first loaded by the caller ahead of time): every
   // chunk, one mask word load per chunk, no per-chunk tests.
   u32 k = m0 + lane;
   u32 q0 = k + 32 < m1 ? (u32)__ldg(Qrow + smd[k + 32].d) : 0u;    // the next round's residue
   if (k < m1) {
-    const MaskDesc md = smd[k];
+    const MaskDesc md = md_first;                    // this lane's stride of the first round
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q) {
       u32 r = q0_first + b[q];
       r = r >= md.s ? r - md.s : r;
       // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
-      const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+      const u32 *wp = tab + q * tab_words + md.off + ((r >> 5) << md.sh);
       const u32 sh = r & 31;
       u32 w0 = wp[0];
       #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const u32 w1 = wp[c + 1];
+        const u32 w1 = wp[(c + 1) << md.sh];
         kill[q][c] = __funnelshift_r(w0, w1, sh);
         w0 = w1;
       }
@@ -360,11 +361,11 @@ __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], 
       for (int q = 0; q < SHORT_LANES; ++q) {
         u32 r = q0 + b[q];
         r = r >= md.s ? r - md.s : r;
-        const u32 *wp = tab + q * tab_words + md.off + (r >> 5);
+        const u32 *wp = tab + q * tab_words + md.off + ((r >> 5) << md.sh);
         const u32 sh = r & 31;
         #pragma unroll
         for (int c = 0; c < NC; ++c)
-          if (alive[q][c]) kill[q][c] = __funnelshift_r(wp[c], wp[c + 1], sh);
+          if (alive[q][c]) kill[q][c] = __funnelshift_r(wp[c << md.sh], wp[(c + 1) << md.sh], sh);
       }
     }
     q0 = q0_next;
@@ -419,8 +420,8 @@ __device__ __forceinline__ u32 short_phase(u32 (&alive)[SHORT_LANES][NC], const 
                                            u32 tab_words, const MaskDesc *smd, u32 m0, u32 m1, u32 l0, u32 l1,
                                            const u32 (&n)[SHORT_LANES], const u32 (&b)[SHORT_LANES],
                                            const u16 *const (&K0row)[SHORT_LANES], const u16 *Qrow, u32 q0_first,
-                                           u32 lane) {
-  const u32 any = short_mask_rounds<NC>(alive, b, tab, tab_words, smd, m0, m1, Qrow, q0_first, lane);
+                                           u32 lane, const MaskDesc &md_first) {
+  const u32 any = short_mask_rounds<NC>(alive, b, tab, tab_words, smd, m0, m1, Qrow, q0_first, lane, md_first);
   if (any && l1 > l0) {
     u32 kill[SHORT_LANES][NC];
     #pragma unroll
@@ -455,7 +456,7 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
                                                const MaskDesc *smd, u32 l_first, const WinRef &R,
                                                const u64 (&rho)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
                                                const u32 (&b)[SHORT_LANES], const u16 *const (&K0row)[SHORT_LANES],
-                                               u32 q0_first, u32 lane) {
+                                               u32 q0_first, u32 lane, const MaskDesc &md0) {
   const u32 wi = R.wi;
   const u16 *Qrow = P.Qm + (size_t)wi * P.Dq;
   u32 alive[SHORT_LANES][NC];
@@ -467,13 +468,14 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
       alive[q][c] = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
     }
   u32 cnt = short_phase<NC>(alive, P, tab, tab_words, smd, 0, P.nm_cov, 0, P.nl_cov, n, b, K0row, Qrow, q0_first,
-                            lane);
+                            lane, md0);
   if (cnt && (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov)) {          // stage B'
     if (lane == 0) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
     const u32 k = P.nm_cov + lane;
     const u32 q0b = k < P.nm_all ? (u32)__ldg(Qrow + smd[k].d) : 0u;
+    const MaskDesc mdb = k < P.nm_all ? smd[k] : MaskDesc{1, 0, 0, 0};
     cnt = short_phase<NC>(alive, P, tab, tab_words, smd, P.nm_cov, P.nm_all, P.nl_cov, P.nl_all, n, b, K0row, Qrow,
-                          q0b, lane);
+                          q0b, lane, mdb);
   }
   if (!cnt) return;
   // survivors are rare: the window's first position index comes from its lane, and lane 0
@@ -538,7 +540,8 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
     // round's stride residue of the next window is loaded while a window is marked.
     constexpr u32 WS = BLOCK / 32;
     const uint4 *sw4 = reinterpret_cast<const uint4 *>(P.shortw);
-    const u32 d_first = lane < P.nm_cov ? smd[lane].d : 0u;
+    const MaskDesc md0 = lane < P.nm_cov ? smd[lane] : MaskDesc{1, 0, 0, 0};   // the first round's stride
+    const u32 d_first = md0.d;
     auto load_q0 = [&](u32 wi) {
       return lane < P.nm_cov ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + d_first) : 0u;
     };
@@ -582,13 +585,13 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
         // instantiations for 1, 2 and 4 chunks (8 too when SEG_SMALL is 256) measured faster
         // than one per chunk count: the kernel's code stays small enough for the instruction
         // cache
-        if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
-        else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+        if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
+        else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
         else if constexpr (SEG_SMALL > 128) {
-          if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
-          else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+          if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
+          else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
         } else if constexpr (SEG_SMALL > 64) {
-          short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane);
+          short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
         }
       }
     }
@@ -610,7 +613,7 @@ __global__ void k_build_masks(const u16 *__restrict__ K0, u32 L, u32 ldk, u32 nf
   if (k0 == K0_MISS) return;
   const MaskDesc md = mdesc[m];
   u32 *row = reinterpret_cast<u32 *>(mtab + (size_t)l * Wpad) + md.off;
-  for (u32 x = k0; x < md.s + SEG_SMALL; x += md.s) atomicOr(row + (x >> 5), 1u << (x & 31));
+  for (u32 x = k0; x < md.s + SEG_SMALL; x += md.s) atomicOr(row + ((x >> 5) << md.sh), 1u << (x & 31));
 }
 
 // Miller-Rabin in two passes. Nearly every survivor is composite and fails the base-2
@@ -665,7 +668,7 @@ constexpr int RUNG_WARPS = ES_RUNG_WARPS;
 #define ES_RUNG_MIN_BLOCKS (16 / RUNG_WARPS)   // resident blocks per SM the register budget allows
 #endif
 #ifndef ES_HELP_BLOCKS_PER_SM
-#define ES_HELP_BLOCKS_PER_SM 1
+#define ES_HELP_BLOCKS_PER_SM 0
 #endif
 #ifndef ES_HELP_BLOCKS_DIV
 #define ES_HELP_BLOCKS_DIV 1
@@ -704,8 +707,10 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   __shared__ unsigned long long next;
   const u64 n = min((u64)*T.prime_count, T.cap);
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ BlockHelp bhelp;
   HardBoard B;
   B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
+  B.local = nullptr;                                 // the warp phase: no block-mates on one prime
   const u64 tail = min(n, (u64)gridDim.x * ES_RUNG_TAIL_PER_BLOCK);
   const u64 nw = n - tail;                           // primes [0, nw): a warp each
   for (;;) {
@@ -715,12 +720,13 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
     if (i >= nw) break;
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
-    const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tde, T.status, F[w], D[w], rho_slot + w, &slot[w], &B,
+    const bool ok = !no_rung && warp_solve_rung(s.p, T.tdp, T.tdi, T.status, F[w], D[w], rho_slot + w, &slot[w], &B,
                                                 T.rho_budget, /*use_ecm=*/false);
     if (lane == 0) rung_result(T, s, si, ok, slot[w]);
     __syncwarp();
   }
   __syncthreads();
+  B.local = &bhelp;
   for (;;) {                                          // primes [nw, n): a block each
     if (threadIdx.x == 0) next = nw + atomicAdd(T.rung_next, 1ull);
     __syncthreads();
@@ -729,7 +735,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
     const bool ok = !no_rung &&
-                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tde, T.status, F, D, rho_slot, &best_k, slot, &res, &B,
+                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tdi, T.status, F, D, rho_slot, &best_k, slot, &res, &B,
                                                  T.rho_budget);
     if (threadIdx.x == 0) rung_result(T, s, si, ok, res);
     __syncthreads();
@@ -738,6 +744,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   // cofactor progress at the issue rate their sub-partition gives them, so helpers beyond
   // one warp per scheduler would only split that rate over more walks, and the expected wait
   // for the first collision grows with the square root of the number of walks sharing it.
+  B.local = nullptr;
   if (!no_rung && blockIdx.x < T.help_blocks) warp_help(B, lane);
 }
 
@@ -782,7 +789,7 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
 }
 __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
-                                                               const TdEntry *tde, u32 *status, u64 rho_budget) {
+                                                               const u64 *tdi, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -790,7 +797,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_probe_r
   __shared__ RungResult slot[RUNG_WARPS];
   __shared__ RungResult res;
   for (u64 i = blockIdx.x; i < count; i += gridDim.x) {
-    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tde, status, F, D, rho_slot, &best_k, slot, &res, nullptr,
+    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tdi, status, F, D, rho_slot, &best_k, slot, &res, nullptr,
                                            rho_budget);
     if (threadIdx.x == 0) {
       if (ok && !check_rung_cert(p[i], res.A, res.r, res.u)) { atomicOr(status, ST_CERT_BAD); ok = false; }
@@ -813,14 +820,14 @@ __global__ void k_probe_direct(const u64 *p, u64 count, RecDev *out, unsigned ch
 }
 // The production factorization (warp_factor), one warp per value; primes sorted ascending.
 __global__ void k_probe_factor(const u64 *n, u64 count, u64 *pr, unsigned char *ex, unsigned char *k,
-                               const u32 *tdp, const TdEntry *tde, u32 *status, u64 rho_budget) {
+                               const u32 *tdp, const u64 *tdi, u32 *status, u64 rho_budget) {
   __shared__ WarpFac F[4];
   __shared__ u64 rho_slot[4];
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const u64 warps = (u64)gridDim.x * blockDim.x / 32;
   for (u64 i = ((u64)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < count; i += warps) {
     WarpFac &f = F[w];
-    const bool ok = warp_factor(n[i], f, tdp, tde, status, lane, rho_slot + w, nullptr, 0, nullptr, rho_budget);
+    const bool ok = warp_factor(n[i], f, tdp, tdi, status, lane, rho_slot + w, nullptr, 0, nullptr, rho_budget);
     if (lane == 0) {
       const int kk = ok ? f.k : 0;
       for (int a = 1; a < kk; ++a)
@@ -938,8 +945,9 @@ struct es_engine {
   es::u64 *d_mtab = nullptr;
   es::MaskDesc *d_mdesc = nullptr;
   es::u32 *d_lfil = nullptr;
-  uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0;
+  uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0, m_inter = 0;
   es::TdEntry *d_tde = nullptr;
+  es::u64 *d_tdi = nullptr;
   // slot 0: es_run_window / es_run_batch / probes; slots 1..SERVE_SLOTS: serving workers
   es::Slot slots[1 + es::SERVE_SLOTS];
   std::string last_error;
@@ -1047,7 +1055,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
   T.help_blocks = (u32)(e->sm_count * ES_HELP_BLOCKS_PER_SM / ES_HELP_BLOCKS_DIV);
   T.rho_budget = e->rho_budget;
-  T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.status = sl->d_status;
+  T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.tdi = e->d_tdi; T.status = sl->d_status;
   T.cap = sl->cap;
   return T;
 }
@@ -1600,6 +1608,7 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_K0, (size_t)L * e->ldk * sizeof(u16)));
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
+  CU(cudaMalloc(&e->d_tdi, tde.size() * sizeof(u64)));
   CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
   temps.p[0] = d_mods;
   CU(cudaMalloc(&d_ress, std::max<size_t>(nf, 1) * sizeof(u64)));
@@ -1617,6 +1626,9 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMemcpyAsync(e->d_sdist, sd.data(), sd.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(e->d_tdp, tdp.data(), tdp.size() * sizeof(u32), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(e->d_tde, tde.data(), tde.size() * sizeof(TdEntry), cudaMemcpyHostToDevice, bs));
+  std::vector<u64> tdi(tde.size());
+  for (size_t i = 0; i < tde.size(); ++i) tdi[i] = tde[i].inv;
+  CU(cudaMemcpyAsync(e->d_tdi, tdi.data(), tdi.size() * sizeof(u64), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_mods, om.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_ress, orr.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice, bs));
@@ -1663,7 +1675,7 @@ static es_status build_tables(es_engine *e) {
         const u32 wd = (st + SEG_SMALL + 31) / 32 + 1;
         if ((size_t)(words + wd) * 4 > MASK_BYTES_MAX || md.size() >= SMD_MAX) break;
         const u32 di = (u32)(std::lower_bound(sd.begin(), sd.end(), st) - sd.begin());
-        md.push_back(MaskDesc{st, di, words, 32 % st});
+        md.push_back(MaskDesc{st, di, words, 0});
         words += wd;
       }
       std::stable_sort(md.begin() + m_first, md.end(),
@@ -1677,6 +1689,25 @@ static es_status build_tables(es_engine *e) {
       if (phase == 0) e->nm_cov = (u32)md.size();
     }
     e->nm_all = (u32)md.size();
+    // Final layout: the first INTERLEAVE_ROUNDS rounds of the covers' phase interleaved (each
+    // group of 32 slices padded to its longest), the rest packed; if that no longer fits the
+    // per-lane budget, fewer rounds are interleaved (the layout cannot change a result).
+    for (u32 rounds = std::min<u32>(INTERLEAVE_ROUNDS, e->nm_cov / 32);; --rounds) {
+      const u32 m_inter = 32 * rounds;
+      u32 w2 = 0;
+      for (u32 g = 0; g < rounds; ++g) {
+        u32 maxwd = 0;
+        for (u32 j = 0; j < 32; ++j) maxwd = std::max(maxwd, (md[32 * g + j].s + SEG_SMALL + 31) / 32 + 1);
+        for (u32 j = 0; j < 32; ++j) { md[32 * g + j].off = w2 + j; md[32 * g + j].sh = 5; }
+        w2 += 32 * maxwd;
+      }
+      for (size_t m = m_inter; m < md.size(); ++m) {
+        md[m].off = w2;
+        md[m].sh = 0;
+        w2 += (md[m].s + SEG_SMALL + 31) / 32 + 1;
+      }
+      if ((size_t)w2 * 4 <= MASK_BYTES_MAX || rounds == 0) { words = w2; e->m_inter = m_inter; break; }
+    }
     e->nl_cov = (u32)lfil_cov.size();
     e->nl_all = (u32)(lfil_cov.size() + lfil_siv.size());
     e->Wpad = std::max<u32>(2, ((words + 1) / 2 + 1) & ~1u);   // in 64-bit words, even
@@ -1707,6 +1738,20 @@ static es_status build_tables(es_engine *e) {
   // The attribute is per function and process-wide: set it to the largest size any engine
   // can ask for (DMAX strides), never to this engine's own size, or a second engine with
   // fewer strides would shrink it under the first.
+  // Stage D's trial division streams its 78 KB prime table once per factorization: ask for
+  // the smallest shared-memory carveout that still holds the resident blocks' static shared
+  // memory, so that the rest of the SM's 256 KB stays L1 and the table stays in it.
+  {
+    int max_smem = 0;
+    CU(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device));
+    for (const void *f : {(const void *)k_rung, (const void *)k_probe_rung}) {
+      cudaFuncAttributes fa;
+      CU(cudaFuncGetAttributes(&fa, f));
+      const double need = (double)ES_RUNG_MIN_BLOCKS * (fa.sharedSizeBytes + 1024);
+      const int pct = std::min(100, (int)(100.0 * need / std::max(max_smem, 1)) + 1);
+      CU(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+    }
+  }
   const size_t smem = mark_smem(e);
   const size_t smem_max = ((4 * DMAX + 15) & ~15u) + std::max<u32>(SEG_BIG, GROUP * SEG_SMALL) + 16;
   CU(cudaFuncSetAttribute(k_mark<MARK_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
@@ -1983,7 +2028,7 @@ es_status es_close(es_engine *e) {
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_tde);
+  cudaFree(e->d_K0); cudaFree(e->d_tde); cudaFree(e->d_tdi);
   cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil);
   delete e;
   return ES_OK;
@@ -2208,7 +2253,7 @@ es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_
   return probe(e, &e->slots[0], count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
                [&](void *in, std::vector<void *> &o) {
                  k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->slots[0].stream>>>((const u64 *)in, count, (RecDev *)o[0],
-                                                                     (unsigned char *)o[1], e->d_tdp, e->d_tde,
+                                                                     (unsigned char *)o[1], e->d_tdp, e->d_tdi,
                                                                      e->slots[0].d_status, e->rho_budget);
                });
 }
@@ -2231,7 +2276,7 @@ es_status es_factor_batch(es_engine *e, const uint64_t *n, size_t count, uint64_
                [&](void *in, std::vector<void *> &o) {
                  k_probe_factor<<<e->sm_count * 4, 128, 0, e->slots[0].stream>>>((const u64 *)in, count, (u64 *)o[0],
                                                                        (unsigned char *)o[1], (unsigned char *)o[2],
-                                                                       e->d_tdp, e->d_tde, e->slots[0].d_status,
+                                                                       e->d_tdp, e->d_tdi, e->slots[0].d_status,
                                                                        e->rho_budget);
                });
 }

@@ -87,7 +87,17 @@ struct MarkParams {
 // read 32 at a time as funnel shifts of consecutive words.
 constexpr u32 MASK_BYTES_MAX = 48 * 1024;   // per-lane mask table budget (shared memory)
 
-struct MaskDesc { u32 s, d, off, c32; };    // stride, its index in sdist, 32-bit word offset, 32 mod s
+// One masked stride: s, its index in sdist, the 32-bit word offset of its slice in a lane's
+// table, and the log2 of the distance between the slice's consecutive words. The strides of
+// the first INTERLEAVE_ROUNDS rounds of 32 (the densest, which every short window walks) are
+// stored interleaved -- word w of the stride in slot 32g + j at off = base_g + j, w at
+// off + 32 w, sh = 5 -- so that lane j of a warp reading any word of its own stride reads
+// shared-memory bank j; the other strides are packed one after another (sh = 0).
+struct MaskDesc { u32 s, d, off, sh; };
+#ifndef ES_INTERLEAVE_ROUNDS
+#define ES_INTERLEAVE_ROUNDS 2
+#endif
+constexpr u32 INTERLEAVE_ROUNDS = ES_INTERLEAVE_ROUNDS;
 
 // A short window as k_mark_short walks it: lanes outside [la, lb) have no position in it.
 // Lane rho holds lq + [(rho - lo) mod M < lr] positions, lq = len / M, lr = len mod M (the
@@ -130,7 +140,8 @@ struct TailParams {
   unsigned long long *rec_count;
   WinCount *cnt;
   const u32 *tdp;          // odd primes < 2^16
-  const TdEntry *tde;
+  const TdEntry *tde;      // their inverses mod 2^64 and division limits (thread-per-value paths)
+  const u64 *tdi;          // their inverses mod 2^64 alone (warp trial division)
   u32 *status;
   u64 cap;                 // capacity of surv/primes/direct/recs
   unsigned long long *rung_next;      // k_rung's prime queue head, whole blocks (the tail)

@@ -139,11 +139,21 @@ struct HardSlot {
   unsigned int state, pad;                     // 0 free, 1 being written, 2 posted
   unsigned long long pad2;
 };
+// A block's own hard cofactor (shared memory): when a warp of a block that works on one
+// prime's rungs has walked rho on a cofactor for RHO_POST_STEPS steps, it posts the cofactor
+// here; block-mates that have finished their own rungs run rounds of elliptic curves on it
+// instead of waiting at the block's barrier, and the first divisor found ends the search.
+struct BlockHelp {
+  unsigned long long n, found;                 // the posted cofactor (0: none), a divisor of it
+  unsigned int busy;                           // warps of the block still on their rungs
+  unsigned int sessions;                       // curve rounds started on the block's cofactors
+};
 struct HardBoard {
   HardSlot *slot;                              // [HARD_SLOTS], all free between runs
   unsigned long long *sessions;                // helping sessions started (distinct constants)
   unsigned long long *done;                    // primes finished by k_rung
   unsigned long long total;                    // primes k_rung has to finish
+  BlockHelp *local;                            // the block's own slot, or null
 };
 
 __device__ __forceinline__ u64 ld_volatile(const unsigned long long *p) { return *(const volatile unsigned long long *)p; }
@@ -217,16 +227,39 @@ __device__ inline u64 warp_ecm(const Mont &M, u64 sigma0, u32 lane, Poll poll, u
 constexpr u64 ECM_AFTER = ES_ECM_AFTER;
 constexpr u32 ECM_OWNER_ROUNDS = 32;     // 1024 curves: a 31-bit factor survives them w.p. ~1e-9
 constexpr u64 ECM_SIGMA_OWNER = 6;       // owner round r: sigma = 6 + 32 r + lane
+constexpr u64 ECM_SIGMA_HELP = 4096;     // helper session t: sigma = 4096 + 32 t + lane
+constexpr u64 ECM_SIGMA_LOCAL = 1ull << 22;   // block-mate session t: sigma = 2^22 + 32 t + lane
+constexpr u32 LOCAL_HELP_POLLS = 1u << 16;   // empty-slot polls (0.5 us apart) before a block-mate stops
+constexpr u32 LOCAL_HELP_ROUNDS = 1u << 12;  // curve rounds per block-mate and prime, at most
+#ifndef ES_LOCAL_HELP
+#define ES_LOCAL_HELP 1
+#endif
+// Helpers on the hard board run rounds of curves (1) or Brent walks (0).
+#ifndef ES_HELP_ECM
+#define ES_HELP_ECM 0
+#endif
 
 __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status, const volatile int *cancel = nullptr,
                                int my_k = 0, const HardBoard *board = nullptr, u64 budget = WARP_RHO_STEPS,
                                bool use_ecm = true) {
   const Mont M = mont_init(n);
   int slot = -1;                                   // the board slot this warp posted n in
+  bool local_posted = false;                       // n is in the block's own slot
   bool stop = false;                               // cancelled (warp-uniform)
+  BlockHelp *const bh = board ? board->local : nullptr;
   auto poll = [&](u64 steps) -> u64 {
     u64 ext = 0;
-    if (lane == 0) {
+    if (lane == 0 && bh) {
+      if (!local_posted && steps >= RHO_POST_STEPS && n < LazyArith::NMAX) {
+        local_posted = atomicCAS(&bh->n, 0ull, (unsigned long long)n) == 0ull;
+        if (local_posted) *(volatile unsigned long long *)&bh->found = 0;   // no divisor of an earlier one
+      }
+      if (local_posted) {
+        const u64 d = *(volatile unsigned long long *)&bh->found;
+        if (d > 1 && d < n && n % d == 0) ext = d;
+      }
+    }
+    if (lane == 0 && !ext) {
       if (cancelled(cancel, my_k)) ext = ~0ull;
       else if (board && slot < 0 && steps >= RHO_POST_STEPS) {
         for (u32 j = 0; j < HARD_SLOTS; ++j)
@@ -270,6 +303,11 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
       if (!f && !stop && steps < budget)
         f = rho_walk<LazyArith>(n, M, 1 + lane + 32 * 1024, 32, budget - steps, lane, poll);
     }
+  }
+  if (lane == 0 && local_posted) {                 // take n out of the block's slot
+    *(volatile unsigned long long *)&bh->found = 0;
+    __threadfence_block();
+    atomicExch(&bh->n, 0ull);
   }
   if (lane == 0 && slot >= 0 && slot < (int)HARD_SLOTS) {  // take n off the board
     atomicExch(&board->slot[slot].state, 1u);
@@ -316,29 +354,109 @@ __device__ inline void warp_help(const HardBoard &B, u32 lane) {
         ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
       return __shfl_sync(FULL, ext, 0);
     };
-    // Helpers walk rho rather than run curves: a helper's walk can stop at any gcd batch and
-    // many walks on one cofactor shorten the wait like 1/sqrt(W), while a curve is a fixed-
-    // length round (helpers running ECM rounds measured 0.51 ms for stage D of the 4096-window
-    // batch against 0.45 ms with rho walks). Constants above every owner's (an owner walks
-    // c = 1 + lane + 32 j with j below 2^12), distinct per session (2^20 sessions apart before
-    // a restart adds 2^25); a posted cofactor has already outlasted its owner's first walks, so
-    // helpers start with a longer window
-    const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
-    const u64 d = n < LazyArith::NMAX ? rho_walk<LazyArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0)
-                                      : rho_walk<ExactArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
+    // With ES_HELP_ECM a helper runs a round of curves, which polls its slot every few ladder
+    // bits and every few giant steps, so it stops as soon as the cofactor is split (rounds that
+    // could not stop early measured worse than rho walks). Otherwise it walks rho: constants
+    // above every owner's (an owner walks c = 1 + lane + 32 j with j below 2^12), distinct per
+    // session (2^20 sessions apart before a restart adds 2^25); a posted cofactor has already
+    // outlasted its owner's first walks, so helpers start with a longer window.
+    u64 d = 0;
+    if (ES_HELP_ECM && n < LazyArith::NMAX) {
+      // A round of 32 curves with sigmas above every owner's (an owner's round r uses
+      // 6 + 32 r + lane, r < ECM_OWNER_ROUNDS), distinct per session; it polls the slot every
+      // few ladder bits, so a helper leaves as soon as anyone has split the cofactor.
+      u64 ext = 0;
+      d = warp_ecm<LazyArith>(M, ECM_SIGMA_HELP + 32 * (ses & 0xFFFFFull), lane, [&]() -> u64 { return poll(0); },
+                              ext);
+    } else {
+      const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
+      d = n < LazyArith::NMAX ? rho_walk<LazyArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0)
+                              : rho_walk<ExactArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
+    }
     if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
       atomicCAS(&hs->found, 0ull, (unsigned long long)d);
     __syncwarp();
   }
 }
 
+// A warp that has finished its rungs helps the block's posted cofactor until every warp of the
+// block has finished: rounds of curves with sigmas of their own (2^22 + 32 t + lane, t the
+// block's session count), each polling the slot every few ladder bits so that it stops as soon
+// as the cofactor is split or withdrawn. Bounded: LOCAL_HELP_POLLS empty polls at most, and
+// every round is bounded. All lanes call.
+__device__ inline void warp_help_block(BlockHelp *bh, u32 lane) {
+  for (u32 idle = 0, rounds = 0; idle < LOCAL_HELP_POLLS && rounds < LOCAL_HELP_ROUNDS;) {
+    u64 n = 0, found = 0;
+    u32 busy = 0;
+    if (lane == 0) {
+      busy = *(volatile unsigned int *)&bh->busy;
+      n = *(volatile unsigned long long *)&bh->n;
+      found = *(volatile unsigned long long *)&bh->found;
+    }
+    busy = __shfl_sync(FULL, busy, 0);
+    if (!busy) return;
+    n = __shfl_sync(FULL, n, 0);
+    found = __shfl_sync(FULL, found, 0);
+    if (!n || found || n >= LazyArith::NMAX || !(n & 1)) { ++idle; __nanosleep(500); continue; }
+    ++rounds;
+    u32 ses = 0;
+    if (lane == 0) ses = atomicAdd(&bh->sessions, 1u);
+    ses = __shfl_sync(FULL, ses, 0);
+    const Mont M = mont_init(n);
+    auto poll = [&]() -> u64 {
+      u64 stop = 0;
+      if (lane == 0)
+        stop = (*(volatile unsigned long long *)&bh->n != n || *(volatile unsigned long long *)&bh->found != 0 ||
+                *(volatile unsigned int *)&bh->busy == 0) ? ~0ull : 0;
+      return __shfl_sync(FULL, stop, 0);
+    };
+    u64 ext = 0;
+    const u64 d = warp_ecm<LazyArith>(M, ECM_SIGMA_LOCAL + 32 * (u64)ses, lane, poll, ext);
+    if (lane == 0 && d > 1 && d < n && n % d == 0 && *(volatile unsigned long long *)&bh->n == n)
+      atomicCAS(&bh->found, 0ull, (unsigned long long)d);
+    __syncwarp();
+  }
+}
+
+// The prime factors of a cofactor v > 2^32 with no prime factor below 2^16 (so at most three
+// of them), appended to F: primes and squares at once, anything else split by warp_rho. All
+// lanes call. Returns false when a bound was hit (status says which) or on cancellation.
+__device__ inline bool warp_factor_cofactor(u64 v0, WarpFac &F, u32 *status, u32 lane, volatile u64 *rho_slot,
+                                            const volatile int *cancel, int my_k, const HardBoard *board,
+                                            u64 rho_budget, bool use_ecm) {
+  u64 stack[4];
+  int sp = 0;
+  stack[sp++] = v0;
+  for (int guard = 0; sp > 0; ++guard) {
+    if (guard > 16) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
+    const u64 v = stack[--sp];
+    if (v == 1) continue;
+    if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;
+    if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
+    const u64 s = isqrt64(v);
+    if (s * s == v) { wf_add(F, s, 2, lane); continue; }
+    const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board, rho_budget, use_ecm);
+    if (d == 0) return false;                  // budget (status set) or cancelled
+    if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
+    stack[sp++] = d;
+    stack[sp++] = v / d;
+  }
+  __syncwarp();
+  if (F.overflow) { if (lane == 0) atomicOr(status, ST_FAC_OVERFLOW); return false; }
+  return true;
+}
+
 // Complete factorization of n >= 1 into F (prime order as found). All lanes call.
-// Returns false when a bound was hit (status says which).
-__device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const TdEntry *__restrict__ tde,
+// Returns false when a bound was hit (status says which). With hard_left, a composite
+// cofactor that would need rho (no prime factor below 2^16, not a square) is not factored:
+// it is left in *hard_left (0 otherwise) and F holds the other prime factors; the caller
+// finishes with warp_factor_cofactor if it needs the rest.
+__device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ tdp, const u64 *__restrict__ tdi,
                                    u32 *status, u32 lane, volatile u64 *rho_slot,
                                    const volatile int *cancel = nullptr, int my_k = 0,
                                    const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
-                                   bool use_ecm = true) {
+                                   bool use_ecm = true, u64 *hard_left = nullptr) {
+  if (hard_left) *hard_left = 0;
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
   if (n <= 1) return true;
@@ -346,26 +464,34 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
   if (tz) { n >>= tz; wf_add(F, 2, tz, lane); }
   u64 cur = n;                 // n with every prime found so far divided out
   bool complete = true;        // every odd prime < 2^16 was tested
-  // Blocks of TD_UNROLL chunks: every table load of a block is issued before any test, so
-  // the block pays one load latency instead of one per chunk. Testing primes past the point
-  // where d^2 > cur is harmless (each prime is tested once, against n, and a hit is a genuine
-  // factor), so the early exit is checked once per block.
+  // Blocks of TD_UNROLL chunks of 32 primes, lane i of chunk c testing prime 32c + i: n is
+  // divisible by an odd prime d iff x = n * d^-1 (mod 2^64) satisfies x * d < 2^64, i.e.
+  // umul64hi(x, d) == 0 (then x = n / d exactly). The table holds only d (tdp) and d^-1 (tdi),
+  // 12 bytes a prime, 78 KB in all, small enough to stay in L1; the loads of the next block
+  // are issued before the current block is tested, so the loop pays one load latency rather
+  // than one per block. Testing primes past the point where d^2 > cur is harmless (each prime
+  // is tested once, against n, and a hit is a genuine factor), so the early exit is checked
+  // once per block.
   constexpr int TD_UNROLL = 8;
-  for (int cb = 0; cb < TD_CHUNKS; cb += TD_UNROLL) {
-    u64 inv[TD_UNROLL], lim[TD_UNROLL];
+  u64 inv[TD_UNROLL], ninv[TD_UNROLL];
+  u32 pr[TD_UNROLL], npr[TD_UNROLL];
+  auto load_block = [&](int cb, u64 (&iv)[TD_UNROLL], u32 (&pv)[TD_UNROLL]) {
     #pragma unroll
     for (int j = 0; j < TD_UNROLL; ++j) {
       const int i = (cb + j) * 32 + lane;
-      if (i < NTD) { const TdEntry t = tde[i]; inv[j] = t.inv; lim[j] = t.lim; }
-      else { inv[j] = 0; lim[j] = 0; }
+      iv[j] = i < NTD ? __ldg(tdi + i) : 0;
+      pv[j] = i < NTD ? __ldg(tdp + i) : 0;
     }
+  };
+  load_block(0, inv, pr);
+  for (int cb = 0; cb < TD_CHUNKS; cb += TD_UNROLL) {
+    if (cb + TD_UNROLL < TD_CHUNKS) load_block(cb + TD_UNROLL, ninv, npr);
     const int nx = (cb + TD_UNROLL) * 32;
-    const u64 dn = nx < NTD ? (u64)__ldg(tdp + nx) : 0;
     #pragma unroll
     for (int j = 0; j < TD_UNROLL; ++j) {
       const int i = (cb + j) * 32 + lane;
       u64 x = n * inv[j];
-      const bool hit = i < NTD && x <= lim[j];
+      const bool hit = i < NTD && __umul64hi(x, (u64)pr[j]) == 0;
       const unsigned mask = __ballot_sync(FULL, hit);
       if (mask) {                                  // rare: a prime below 2^16 divides n
         u64 f = 1;
@@ -376,7 +502,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
           f = inv[j];
           for (int g = 0; g < 64; ++g) {
             x = m * inv[j];
-            if (x > lim[j]) break;
+            if (__umul64hi(x, (u64)pr[j])) break;
             m = x; ++e; f *= inv[j];
           }
         }
@@ -384,7 +510,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
         __syncwarp();
         if (hit) {
           const int pos = base + __popc(mask & ((1u << lane) - 1));
-          if (pos < MAXF) { F.pr[pos] = __ldg(tdp + i); F.ex[pos] = e; }
+          if (pos < MAXF) { F.pr[pos] = pr[j]; F.ex[pos] = e; }
         }
         u64 g = f;
         #pragma unroll
@@ -400,31 +526,22 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
       }
     }
     if (nx >= NTD) break;
+    const u64 dn = __shfl_sync(FULL, (u64)npr[0], 0);   // the next block's first prime
     if (dn * dn > cur) { complete = false; break; }   // cur is 1 or prime
     if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;   // moot rung
+    #pragma unroll
+    for (int j = 0; j < TD_UNROLL; ++j) { inv[j] = ninv[j]; pr[j] = npr[j]; }
   }
   if (cur > 1) {
     if (!complete || cur <= 0xFFFFFFFFull) {
       wf_add(F, cur, 1, lane);
+    } else if (hard_left) {
+      const u64 s = isqrt64(cur);
+      if (warp_is_prime(cur, lane)) wf_add(F, cur, 1, lane);
+      else if (s * s == cur) wf_add(F, s, 2, lane);     // s is prime: no factor of cur is below 2^16
+      else *hard_left = cur;                             // needs rho: left to the caller
     } else {
-      // cur > 2^32 with no prime factor below 2^16: at most three prime factors.
-      u64 stack[4];
-      int sp = 0;
-      stack[sp++] = cur;
-      for (int guard = 0; sp > 0; ++guard) {
-        if (guard > 16) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
-        const u64 v = stack[--sp];
-        if (v == 1) continue;
-        if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;
-        if (v <= 0xFFFFFFFFull || warp_is_prime(v, lane)) { wf_add(F, v, 1, lane); continue; }
-        const u64 s = isqrt64(v);
-        if (s * s == v) { wf_add(F, s, 2, lane); continue; }
-        const u64 d = warp_rho(v, lane, rho_slot, status, cancel, my_k, board, rho_budget, use_ecm);
-        if (d == 0) return false;                  // budget (status set) or cancelled
-        if (sp + 2 > 4) { if (lane == 0) atomicOr(status, ST_STACK_OVERFLOW); return false; }
-        stack[sp++] = d;
-        stack[sp++] = v / d;
-      }
+      return warp_factor_cofactor(cur, F, status, lane, rho_slot, cancel, my_k, board, rho_budget, use_ecm);
     }
   }
   __syncwarp();
@@ -492,6 +609,38 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
 
 struct RungResult { u64 A; u32 r, k; U128 u; };
 
+// Below this bound a divisor of q^2 = (pA)^2 cannot involve p or a prime factor of a cofactor
+// that trial division left (every such prime is at least 65537, the first prime after the
+// trial-division table's last, 65521).
+constexpr u64 SMALL_U_BOUND = 65536;
+#ifndef ES_SMALL_U
+#define ES_SMALL_U 1
+#endif
+
+// min_div_res of one rung (sieve/rung_scan3.cpp:544-565): the least divisor u <= q of q^2,
+// q = pA, with u == target (mod r), or u = 0 when there is none. A is factored by trial
+// division first; when that leaves a composite cofactor C (prime factors all >= 65537), the
+// divisors of q^2 below 65537 are exactly those of S^2, S = A / C, so the least qualifying
+// one among them -- found from S's primes alone -- is the answer whenever it exists, and C is
+// factored (rho, ECM) only when it does not. The same u comes out either way. Returns false
+// when a bound was hit or the rung was cancelled.
+__device__ inline bool rung_divisor(u64 p, u64 A, U128 q, u32 r, u32 target, WarpFac &F, DPWarp &D,
+                                    const u32 *tdp, const u64 *tdi, u32 *status, u32 lane,
+                                    volatile u64 *rho_slot, const volatile int *cancel, int my_k,
+                                    const HardBoard *board, u64 rho_budget, bool use_ecm, U128 &u) {
+  u64 hard = 0;
+  if (!warp_factor(A, F, tdp, tdi, status, lane, rho_slot, cancel, my_k, board, rho_budget, use_ecm,
+                   ES_SMALL_U ? &hard : nullptr))
+    return false;
+  if (hard) {
+    u = warp_min_div_res(p, F, U128{SMALL_U_BOUND, 0}, r, target, D, lane);
+    if (u.lo || u.hi) return true;
+    if (!warp_factor_cofactor(hard, F, status, lane, rho_slot, cancel, my_k, board, rho_budget, use_ecm)) return false;
+  }
+  u = warp_min_div_res(p, F, q, r, target, D, lane);
+  return true;
+}
+
 // The rung walk of one prime by one warp, rung after rung (solve_rung3,
 // sieve/rung_scan3.cpp:578-603, in its own order): the throughput form of block_solve_rung
 // below, for while there are more primes than warps. Returns true in every lane when a rung
@@ -499,7 +648,7 @@ struct RungResult { u64 A; u32 r, k; U128 u; };
 // cofactors on rho: with every warp of the GPU busy, a round of curves costs more issue slots
 // than the rho steps it saves (a 10^14-integer window at 10^16, a million primes: 108 ms of
 // stage D with rho alone, 179 ms with ECM), while ECM pays in the latency-bound tail.
-__device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac &F,
+__device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u32 *status, WarpFac &F,
                                        DPWarp &D, volatile u64 *rho_slot, RungResult *out,
                                        const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
                                        bool use_ecm = true) {
@@ -514,9 +663,11 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F, tdp, tde, status, lane, rho_slot, nullptr, 0, board, rho_budget, use_ecm)) return false;
     const U128 q{p * A, __umul64hi(p, A)};
-    const U128 u = warp_min_div_res(p, F, q, r, target, D, lane);
+    U128 u;
+    if (!rung_divisor(p, A, q, r, target, F, D, tdp, tdi, status, lane, rho_slot, nullptr, 0, board, rho_budget,
+                      use_ecm, u))
+      return false;
     if (u.lo == 0 && u.hi == 0) continue;
     if (lane == 0) *out = RungResult{A, r, k, u};
     __syncwarp();
@@ -529,11 +680,15 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde
 // stops once k passes the best certifying index found by any warp. Returns true in every
 // thread when some rung certifies p; the block's result is then in *out.
 template <int W>
-__device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *tde, u32 *status, WarpFac *F, DPWarp *D,
+__device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u32 *status, WarpFac *F, DPWarp *D,
                                  volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out,
                                  const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (threadIdx.x == 0) *best_k = 0x7FFFFFFF;
+  BlockHelp *const bh = board ? board->local : nullptr;
+  if (threadIdx.x == 0) {
+    *best_k = 0x7FFFFFFF;
+    if (bh) { bh->n = 0; bh->found = 0; bh->busy = W; }
+  }
   if (lane == 0) slot[w].k = 0x7FFFFFFF;
   __syncthreads();
   const u32 pm4 = (u32)(p & 3);
@@ -548,15 +703,22 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const TdEntry *td
     const u32 qm = (u32)(((p % r) * (A % r)) % r);
     if (r > 1 && gcd64(qm, r) != 1) continue;
     const u32 target = qm ? r - qm : 0;
-    if (!warp_factor(A, F[w], tdp, tde, status, lane, rho_slot + w, best_k, (int)k, board, rho_budget)) break;
     const U128 q{p * A, __umul64hi(p, A)};
-    const U128 u = warp_min_div_res(p, F[w], q, r, target, D[w], lane);
+    U128 u;
+    if (!rung_divisor(p, A, q, r, target, F[w], D[w], tdp, tdi, status, lane, rho_slot + w, best_k, (int)k, board,
+                      rho_budget, true, u))
+      break;
     if (u.lo == 0 && u.hi == 0) continue;
     if (lane == 0) {
       slot[w] = RungResult{A, r, k, u};
       atomicMin(best_k, (int)k);
     }
     break;
+  }
+  if (bh) {                                     // done with this prime's rungs: help the others
+    if (lane == 0) atomicSub(&bh->busy, 1u);
+    __syncwarp();
+    if (ES_LOCAL_HELP) warp_help_block(bh, lane);
   }
   __syncthreads();
   const int bk = *(volatile int *)best_k;
