@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--serve", type=int, default=2000, help="serving requests (0: no serving leg)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule")
+    ap.add_argument("--no-batch19", action="store_true", help="skip the batch at [1e19, ceiling)")
     return ap.parse_args()
 
 
@@ -224,18 +225,24 @@ def integers(wins):
 
 
 def l2_flusher(device):
-    """A 256 MB device buffer rewritten before every timed step (larger than the 129 MB L2)."""
+    """A 256 MB device buffer rewritten before every timed step (larger than the 129 MB L2).
+    flush() waits for the write; flush_async() only queues it (on torch's stream, which the
+    engine's streams do not wait for), for the pipelined leg, where a wait would drain the
+    batches in flight."""
     try:
         import torch
         buf = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda:%d" % device)
 
-        def flush(k=[0]):
+        def flush_async(k=[0]):
             k[0] += 1
             buf.fill_(k[0])
+
+        def flush():
+            flush_async()
             torch.cuda.synchronize(device)
-        return flush, "flushed (256 MB write before each timed step)"
+        return flush, flush_async, "flushed (256 MB write before each timed step)"
     except Exception as ex:  # torch missing: say so rather than hide it
-        return (lambda: None), "not flushed (%s)" % type(ex).__name__
+        return (lambda: None), (lambda: None), "not flushed (%s)" % type(ex).__name__
 
 
 def cpu_baseline(wins, seconds, threads=None):
@@ -346,9 +353,60 @@ def serve_leg(eng, n, seed):
             "busy_refusals": refused[0]}
 
 
+def sync_leg(eng, wins, steps, flush):
+    """`steps` synchronous es_run_batch calls from host buffers, L2 flushed before each: the
+    device time of each call's kernels (es_timing, CUDA events on the engine's stream) and the
+    wall time of the call."""
+    out = {"dev_ms": 0.0, "wall_s": 0.0, "launches": 0, "recs": 0,
+           "stage": {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0},
+           "kern": {"prep_ms": 0.0, "mark_short_ms": 0.0, "mark_long_ms": 0.0},
+           "host": {"host_setup_ms": 0.0, "host_device_ms": 0.0, "host_collect_ms": 0.0, "host_total_ms": 0.0}}
+    warr, carr = eng.make_windows(wins), eng.make_counters(len(wins))
+    for _ in range(steps):
+        flush()
+        t0 = time.perf_counter()
+        nrec = eng.run_batch_c(warr, len(wins), carr)     # es_run_batch: host buffers in and out
+        out["wall_s"] += time.perf_counter() - t0
+        t = eng.timing()
+        out["last"] = t
+        out["dev_ms"] += t["total_ms"]
+        out["launches"] += int(t["kernel_launches"])
+        out["recs"] = max(out["recs"], nrec)
+        for grp in ("stage", "kern", "host"):
+            for k in out[grp]:
+                out[grp][k] += t[k]
+    return out
+
+
+def pipelined_leg(eng, wins, steps, warmup, flush_async, depth=3):
+    """`steps` batches through es_submit_batch / es_poll from host buffers, `depth` of them
+    submitted at a time: the engine's two serving streams each run one, marking one batch
+    while the other's stage D finishes. A 256 MB L2-flushing write is queued before every
+    submission (on another stream: it runs beside the batches in flight and competes with
+    them). Returns (wall seconds of the timed steps, the largest record count of a step)."""
+    from collections import deque
+    n = len(wins)
+    warr = eng.make_windows(wins)
+    carrs = [eng.make_counters(n) for _ in range(depth)]
+
+    def run(k):
+        q, recs = deque(), 0
+        t0 = time.perf_counter()
+        for i in range(k):
+            flush_async()
+            q.append(eng.submit_batch_c(warr, n))
+            if len(q) >= depth:
+                recs = max(recs, eng.poll_c(q.popleft(), carrs[i % depth]))
+        while q:
+            recs = max(recs, eng.poll_c(q.popleft(), carrs[0]))
+        return time.perf_counter() - t0, recs
+    run(max(warmup, 2 * depth))
+    return run(steps)
+
+
 def run_gpu(args, ws, rank, local):
     import es_sieve
-    flush, flush_note = l2_flusher(local)
+    flush, flush_async, flush_note = l2_flusher(local)
     mods, ress = es_sieve.load_filters(GPU_TABLE)
     eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local, sieve_p=args.sieve)
     wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
@@ -357,45 +415,30 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.warmup):
         eng.run_batch(wins)
     barrier(ws)
-    dev_ms, wall_s, launches, recs_n, items = 0.0, 0.0, 0, 0, 0
-    stage = {"mark_ms": 0.0, "mr_ms": 0.0, "rung_ms": 0.0, "direct_ms": 0.0}
-    kern = {"prep_ms": 0.0, "mark_short_ms": 0.0, "mark_long_ms": 0.0}
-    host = {"host_setup_ms": 0.0, "host_device_ms": 0.0, "host_collect_ms": 0.0, "host_total_ms": 0.0}
-    warr, carr = eng.make_windows(wins), eng.make_counters(len(wins))
     with Clocks(local) as clk:
-        for _ in range(args.steps):
-            flush()
-            t0 = time.perf_counter()
-            nrec = eng.run_batch_c(warr, len(wins), carr)     # es_run_batch: host buffers in and out
-            wall_s += time.perf_counter() - t0
-            t = eng.timing()
-            last_t = t
-            dev_ms += t["total_ms"]
-            launches += int(t["kernel_launches"])
-            items = int(t["mark_items"])
-            recs_n = nrec
-            for k in stage:
-                stage[k] += t[k]
-            for k in kern:
-                kern[k] += t[k]
-            for k in host:
-                host[k] += t[k]
+        sy = sync_leg(eng, wins, args.steps, flush)
+        pipe_wall, pipe_recs = pipelined_leg(eng, wins, args.steps, args.warmup, flush_async)
     barrier(ws)
     clocks = clk.summary()
+    dev_ms, wall_s, launches, recs_n = sy["dev_ms"], sy["wall_s"], sy["launches"], sy["recs"]
+    stage, kern, host, last_t = sy["stage"], sy["kern"], sy["host"], sy["last"]
     dev_s = allmax(ws, dev_ms / 1000.0)
     wall = allmax(ws, wall_s)
+    pipe = allmax(ws, pipe_wall)
     total_int = allsum(ws, n_int * args.steps)
     value = total_int / dev_s
-    e2e = total_int / wall
+    e2e_sync = total_int / wall
+    e2e = total_int / pipe
     extra = {}
     if not args.no_plain:
         flush()
-        per_p, _ = eng.run_batch(wins, schedule=es_sieve.ES_SCHED_PLAIN)
+        per_p, rec_p = eng.run_batch(wins, schedule=es_sieve.ES_SCHED_PLAIN)
         tp = eng.timing()
         extra["plain"] = {"value": n_int / (tp["total_ms"] / 1000.0), "ms_per_step": tp["total_ms"],
                           "kernel_launches": int(tp["kernel_launches"])}
-        per_b, _ = eng.run_batch(wins)
-        extra["plain"]["records_identical"] = per_p == per_b
+        per_b, rec_b = eng.run_batch(wins)
+        extra["plain"]["counters_identical"] = per_p == per_b
+        extra["plain"]["records_identical"] = rec_p.tobytes() == rec_b.tobytes()
         c3 = workloads.c3()
         eng.run_window(c3["lo"], c3["hi"])
         flush()
@@ -403,6 +446,28 @@ def run_gpu(args, ws, rank, local):
         t3 = eng.timing()
         extra["c3"] = {"value": (c3["hi"] - c3["lo"]) / (t3["total_ms"] / 1000.0), "ms_per_step": t3["total_ms"],
                        "lo": c3["lo"], "mark_ms": t3["mark_ms"], "rung_ms": t3["rung_ms"]}
+    if not args.no_batch19:
+        # the same batch law at the top of the range, [1e19, DIRECT_PMAX): same engine and schedule
+        w19 = workloads.batch19_windows(args.windows, seed=workloads.SEED + rank)
+        n19 = integers(w19)
+        for _ in range(args.warmup):
+            eng.run_batch(w19)
+        s19 = sync_leg(eng, w19, args.steps, flush)
+        p19, _ = pipelined_leg(eng, w19, args.steps, args.warmup, flush_async)
+        b19 = {"windows": len(w19), "integers_per_step": n19,
+               "value": n19 * args.steps / (s19["dev_ms"] / 1000.0), "ms_per_step": s19["dev_ms"] / args.steps,
+               "stages_ms_per_step": dict({k: v / args.steps for k, v in s19["stage"].items()},
+                                          **{k: v / args.steps for k, v in s19["kern"].items()}),
+               "primes": int(s19["last"]["primes"]),
+               "e2e": {"value": n19 * args.steps / p19, "mode": "pipelined (es_submit_batch / es_poll, 3 in flight)"},
+               "e2e_sync": {"value": n19 * args.steps / s19["wall_s"], "mode": "es_run_batch"}}
+        if not args.no_plain:
+            flush()
+            eng.run_batch(w19, schedule=es_sieve.ES_SCHED_PLAIN, records=False)
+            tp = eng.timing()
+            b19["plain"] = {"value": n19 / (tp["total_ms"] / 1000.0), "ms_per_step": tp["total_ms"],
+                            "kernel_launches": int(tp["kernel_launches"])}
+        extra["batch19"] = b19
     if args.serve:
         serve_leg(eng, min(200, args.serve), workloads.SEED + 7)          # warm the serving slots
         extra["serve"] = serve_leg(eng, args.serve, workloads.SEED + 1000 * (rank + 1))
@@ -474,8 +539,15 @@ def run_gpu(args, ws, rank, local):
                 # counters, status, per-window counters and records out (pinned staging; the
                 # graph copies the first 4096 record slots back every run, any more afterwards)
                 "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),
-                        "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * max(recs_n, 4096)},
-                "gpu_launches": launches, "clocks": clocks, "roofline": roof, "cpu_baseline": cpu,
+                        "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * max(pipe_recs, 4096),
+                        "mode": "pipelined: es_submit_batch / es_poll, 3 batches in flight, host buffers in and out",
+                        "ms_per_step": 1000.0 * pipe / args.steps},
+                "e2e_sync": {"value": e2e_sync, "unit": "integers/s", "mode": "es_run_batch, one call per step",
+                             "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),
+                             "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * max(recs_n, 4096),
+                             "ms_per_step": 1000.0 * wall / args.steps},
+                "gpu_launches": launches + int(last_t["kernel_launches"]) * args.steps, "clocks": clocks,
+                "roofline": roof, "cpu_baseline": cpu,
                 "stages_ms_per_step": dict({k: v / args.steps for k, v in stage.items()},
                                            **{k: v / args.steps for k, v in kern.items()}),
                 "tail": {"survivors": int(last_t["survivors"]), "primes": int(last_t["primes"])},

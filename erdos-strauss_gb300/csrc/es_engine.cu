@@ -870,8 +870,13 @@ struct Slot {
   unsigned long long *h_ctr = nullptr;
   u32 *h_status = nullptr;
   RecDev *h_recs = nullptr;
-  cudaGraph_t graph = nullptr;          // the persistent schedule, captured once per capacity
-  cudaGraphExec_t gexec = nullptr;
+  // The persistent schedule, captured once per capacity as two graphs: the front (counters
+  // cleared, staging copied in, marking, Miller-Rabin) and the tail (stage D, stage E,
+  // counters and the record prefix copied out). ev[11] is recorded between them on the
+  // slot's stream: the next slot's front waits for it (marking runs one batch at a time, in
+  // launch order) while this slot's tail overlaps the next batch's marking.
+  cudaGraph_t graph = nullptr, graph2 = nullptr;
+  cudaGraphExec_t gexec = nullptr, gexec2 = nullptr;
   WinDev *d_win = nullptr; size_t win_cap = 0;
   WinCount *d_cnt = nullptr;
   ShortWin *d_shortw = nullptr; size_t shortw_cap = 0;
@@ -915,6 +920,7 @@ struct Request {
   std::string err;
   bool done = false;
   bool claimed = false;                 // an es_poll is waiting on it (one poller per ticket)
+  bool solo = false;                    // es_submit_batch: runs as a batch of its own
   u64 mem = 0;                          // admitted device-memory estimate
 };
 }  // namespace es
@@ -964,6 +970,10 @@ struct es_engine {
   int pollers = 0;                      // es_poll calls inside the engine (es_close waits for them)
   std::vector<std::thread> workers;
   bool stopping = false;
+  // persistent runs of every slot: the slot whose front graph was launched last (its ev[11]
+  // marks the end of that front), so that fronts run one after another in launch order
+  std::mutex front_mu;
+  es::Slot *last_front = nullptr;
 };
 
 namespace es {
@@ -983,8 +993,10 @@ static es_status fail(es_engine *e, es_status s, const std::string &msg) {
 static void drop_graph(Slot *sl) {
   if (sl->gexec) cudaGraphExecDestroy(sl->gexec);
   if (sl->graph) cudaGraphDestroy(sl->graph);
-  sl->gexec = nullptr;
-  sl->graph = nullptr;
+  if (sl->gexec2) cudaGraphExecDestroy(sl->gexec2);
+  if (sl->graph2) cudaGraphDestroy(sl->graph2);
+  sl->gexec = sl->gexec2 = nullptr;
+  sl->graph = sl->graph2 = nullptr;
 }
 
 // Device buffers for nwin windows and a survivor capacity of cap, with their pinned host
@@ -1162,8 +1174,10 @@ static u64 positions_in(const es_engine *e, u64 lo, u64 hi) {
 // tail, and the copies of the run counters back to pinned memory. With `capture` the event
 // records are external graph nodes, so that the kernels can still be timed when the
 // sequence runs as a graph. `items_hint` sizes k_mark's grid for the plain schedule.
-static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCount *cnt, size_t ncopy, size_t nshort_copy,
-                                u64 items_hint, bool capture) {
+// The funnel's front on the slot's stream: run counters cleared, batch header and window
+// descriptors copied in, residues, marking (short and long windows), Miller-Rabin.
+static es_status enqueue_front(es_engine *e, Slot *sl, bool persistent, WinCount *cnt, size_t ncopy, size_t nshort_copy,
+                               u64 items_hint, bool capture) {
   MarkParams P = mark_params(e, sl);
   TailParams T = tail_params(e, sl);
   P.cnt = cnt;
@@ -1202,6 +1216,17 @@ static es_status enqueue_funnel(es_engine *e, Slot *sl, bool persistent, WinCoun
   k_mr2<<<e->sm_count * 2, 256, 0, st>>>(T);
   CU(cudaGetLastError());
   CU(rec(2));
+  return ES_OK;
+}
+
+// The funnel's tail on the slot's stream: stage D, stage E, run counters and status copied out.
+static es_status enqueue_tail(es_engine *e, Slot *sl, WinCount *cnt, bool capture) {
+  TailParams T = tail_params(e, sl);
+  T.cnt = cnt;
+  cudaStream_t st = sl->stream;
+  auto rec = [&](int k) {
+    return capture ? cudaEventRecordWithFlags(sl->ev[k], st, cudaEventRecordExternal) : cudaEventRecord(sl->ev[k], st);
+  };
   k_rung<<<e->sm_count * e->sched.rung_blocks_per_sm, RUNG_WARPS * 32, 0, st>>>(T, (e->flags & ES_FLAG_NO_RUNG) ? 1 : 0);
   CU(cudaGetLastError());
   CU(rec(3));
@@ -1219,27 +1244,53 @@ constexpr size_t REC_PREFIX = 4096;
 
 static es_status capture_graph(es_engine *e, Slot *sl) {
   drop_graph(sl);
+  // the front: per-window counters cleared, then the funnel up to Miller-Rabin
   CU(cudaStreamBeginCapture(sl->stream, cudaStreamCaptureModeThreadLocal));
   es_status s = ES_OK;
   const cudaError_t m = cudaMemsetAsync(sl->d_cnt, 0, sl->win_cap * sizeof(WinCount), sl->stream);
-  if (m == cudaSuccess) s = enqueue_funnel(e, sl, true, sl->d_cnt, sl->win_cap, sl->shortw_cap, 0, true);
-  // The graph also copies back the first REC_PREFIX record slots, so that a batch with fewer
-  // records (every 4096-window batch at 1e19 has about 1.6 K) needs no copy after the run.
+  if (m == cudaSuccess) s = enqueue_front(e, sl, true, sl->d_cnt, sl->win_cap, sl->shortw_cap, 0, true);
+  cudaGraph_t g = nullptr;
+  cudaError_t end = cudaStreamEndCapture(sl->stream, &g);
+  if (m != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(m));
+  if (s != ES_OK) { if (g) cudaGraphDestroy(g); return s; }
+  if (end != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(end));
+  sl->graph = g;
+  CU(cudaGraphInstantiate(&sl->gexec, g, 0));
+  // the tail: stage D and E, then the counters and the first REC_PREFIX record slots copied
+  // back, so that a batch with fewer records (every 4096-window batch at 1e19 has about
+  // 1.6 K) needs no copy after the run
+  CU(cudaStreamBeginCapture(sl->stream, cudaStreamCaptureModeThreadLocal));
+  s = enqueue_tail(e, sl, sl->d_cnt, true);
   sl->rec_prefix = std::min<size_t>(sl->cap, REC_PREFIX);
-  if (m == cudaSuccess && s == ES_OK) {
+  if (s == ES_OK) {
     cudaError_t c2 = cudaMemcpyAsync(sl->h_cnt, sl->d_cnt, sl->win_cap * sizeof(WinCount),
                                      cudaMemcpyDeviceToHost, sl->stream);
     if (c2 == cudaSuccess)
       c2 = cudaMemcpyAsync(sl->h_recs, sl->d_recs, sl->rec_prefix * sizeof(RecDev), cudaMemcpyDeviceToHost, sl->stream);
     if (c2 != cudaSuccess) s = fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(c2));
   }
-  cudaGraph_t g = nullptr;
-  const cudaError_t end = cudaStreamEndCapture(sl->stream, &g);
-  if (m != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(m));
+  g = nullptr;
+  end = cudaStreamEndCapture(sl->stream, &g);
   if (s != ES_OK) { if (g) cudaGraphDestroy(g); return s; }
   if (end != cudaSuccess) return fail(e, ES_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(end));
-  sl->graph = g;
-  CU(cudaGraphInstantiate(&sl->gexec, g, 0));
+  sl->graph2 = g;
+  CU(cudaGraphInstantiate(&sl->gexec2, g, 0));
+  return ES_OK;
+}
+
+// Launches a captured persistent run on the slot's stream. The front waits for the front
+// most recently launched on any other slot, so batches are marked one at a time in launch
+// order, and a batch's stage-D tail (a few latency-bound factorizations on a handful of SMs)
+// runs beside the next batch's marking instead of leaving the GPU idle.
+static es_status launch_persistent(es_engine *e, Slot *sl) {
+  {
+    std::lock_guard<std::mutex> lk(e->front_mu);
+    if (e->last_front && e->last_front != sl) CU(cudaStreamWaitEvent(sl->stream, e->last_front->ev[11], 0));
+    CU(cudaGraphLaunch(sl->gexec, sl->stream));
+    CU(cudaEventRecord(sl->ev[11], sl->stream));
+    e->last_front = sl;
+  }
+  CU(cudaGraphLaunch(sl->gexec2, sl->stream));
   return ES_OK;
 }
 
@@ -1341,10 +1392,11 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
         for (int b = 1; b < 34; ++b) start[b] += start[b - 1];
         for (size_t k = 0; k < ns; ++k) sl->h_short[start[32 - mag[k]]++] = shortw[k];
       }
-      if (!sl->gexec) { s = capture_graph(e, sl); if (s) return s; }
+      if (!sl->gexec || !sl->gexec2) { s = capture_graph(e, sl); if (s) return s; }
       setup_ms = ms_since(t_start);
       const auto t_launch = std::chrono::steady_clock::now();
-      CU(cudaGraphLaunch(sl->gexec, sl->stream));
+      s = launch_persistent(e, sl);
+      if (s) return s;
       CU(cudaStreamSynchronize(sl->stream));
       device_ms = ms_since(t_launch);
       launches = 7;
@@ -1362,7 +1414,9 @@ static es_status run_device_windows(es_engine *e, Slot *sl, const es_window *w, 
         u32 nshort = 0;
         if (k < shortw.size() && shortw[k].wi == i) { sl->h_short[0] = shortw[k++]; sl->h_short[0].wi = 0; nshort = 1; }
         sl->h_hdr->total_items = items; sl->h_hdr->nwin = 1; sl->h_hdr->nshort = nshort;
-        s = enqueue_funnel(e, sl, false, sl->d_cnt + i, 1, nshort, items, false);
+        s = enqueue_front(e, sl, false, sl->d_cnt + i, 1, nshort, items, false);
+        if (s) return s;
+        s = enqueue_tail(e, sl, sl->d_cnt + i, false);
         if (s) return s;
         CU(cudaStreamSynchronize(sl->stream));
         launches += 7;
@@ -1788,7 +1842,10 @@ static void serve_worker(es_engine *e, int k) {
       e->qcv.wait(lk, [&] { return e->stopping || !e->queue.empty(); });
       if (e->stopping && e->queue.empty()) return;
       size_t nw = 0;
-      while (!e->queue.empty() && (batch.empty() || nw + e->queue.front()->w.size() <= SERVE_BATCH_WINDOWS)) {
+      // a solo request (es_submit_batch) is a batch of its own, of any size
+      while (!e->queue.empty() &&
+             (batch.empty() || (!batch[0]->solo && !e->queue.front()->solo &&
+                                nw + e->queue.front()->w.size() <= SERVE_BATCH_WINDOWS))) {
         Request *r = e->queue.front();
         e->queue.pop_front();
         nw += r->w.size();
@@ -2291,7 +2348,7 @@ es_status es_check_records(es_engine *e, const es_record *r, size_t count, uint8
                });
 }
 
-es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket) {
+static es_status submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket, bool solo) {
   if (!e || !ticket || (!w && n)) return ES_ERR_ARG;
   *ticket = 0;
   const u64 floor_ = std::max(e->wheel_pmin, e->cover_pmax);
@@ -2302,6 +2359,7 @@ es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket
   Request *r = new (std::nothrow) Request();
   if (!r) return ES_ERR_NOMEM;
   r->w.assign(w, w + n);
+  r->solo = solo;
   r->mem = request_bytes(e, w, n);
   {
     std::lock_guard<std::mutex> lk(e->qmu);
@@ -2323,6 +2381,14 @@ es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket
   }
   e->qcv.notify_one();
   return ES_OK;
+}
+
+es_status es_submit(es_engine *e, const es_window *w, size_t n, uint64_t *ticket) {
+  return submit(e, w, n, ticket, false);
+}
+
+es_status es_submit_batch(es_engine *e, const es_window *w, size_t n, uint64_t *ticket) {
+  return submit(e, w, n, ticket, true);
 }
 
 es_status es_poll(es_engine *e, uint64_t ticket, es_counters *per_window, es_records *recs, int timeout_ms) {

@@ -108,6 +108,7 @@ def load_library(path=LIB_PATH):
         "es_run_window": (C.c_int, [e, C.c_uint64, C.c_uint64, P(Counters), P(Records)]),
         "es_run_batch": (C.c_int, [e, P(Window), C.c_size_t, C.c_int, P(Counters), P(Records)]),
         "es_submit": (C.c_int, [e, P(Window), C.c_size_t, P(C.c_uint64)]),
+        "es_submit_batch": (C.c_int, [e, P(Window), C.c_size_t, P(C.c_uint64)]),
         "es_poll": (C.c_int, [e, C.c_uint64, P(Counters), P(Records), C.c_int]),
         "es_free_records": (C.c_int, [P(Records)]),
         "es_format_record": (C.c_size_t, [P(Record), C.c_char_p, C.c_size_t]),
@@ -305,6 +306,27 @@ class Engine:
         t = C.c_uint64()
         self._check(self.lib.es_submit(self.h, w, n, C.byref(t)))
         return t.value
+
+    def submit_batch(self, windows):
+        """Queue windows as one batch of their own (es_submit_batch); returns a ticket for poll()."""
+        n = len(windows)
+        w = self.make_windows(windows)
+        return self.submit_batch_c(w, n)
+
+    # The C calls alone, for timing: a caller-built window array (make_windows) in, a
+    # caller-built counter array (make_counters) filled, records freed here.
+    def submit_batch_c(self, warr, n):
+        t = C.c_uint64()
+        self._check(self.lib.es_submit_batch(self.h, warr, n, C.byref(t)))
+        return t.value
+
+    def poll_c(self, ticket, carr, timeout_ms=-1):
+        """es_poll into carr; returns the record count."""
+        r = Records()
+        self._check(self.lib.es_poll(self.h, ticket, carr, C.byref(r), timeout_ms))
+        nrec = r.n
+        self.lib.es_free_records(C.byref(r))
+        return nrec
 
     def poll(self, ticket, n, timeout_ms=-1):
         """(per-window counters, records) of a submitted request; EsError(ES_ERR_TIMEOUT) if not done."""

@@ -175,6 +175,14 @@ es_status es_run_batch(es_engine *engine, const es_window *w, size_t n, int sche
 es_status es_submit(es_engine *engine, const es_window *w, size_t n, uint64_t *ticket);
 es_status es_poll(es_engine *engine, uint64_t ticket, es_counters *per_window, es_records *recs,
                   int timeout_ms);
+/* The asynchronous form of es_run_batch (persistent schedule): the windows are queued as one
+ * batch of their own (never merged with other requests, any number of windows) and collected
+ * with es_poll like any ticket. Batches are marked one at a time in the order the serving
+ * streams launch them, and each batch's stage D (a few latency-bound factorizations at the end
+ * of its run) overlaps the next batch's marking, so a caller that keeps two batches submitted
+ * verifies more integers/s than one calling es_run_batch in a loop. Admission as es_submit.
+ * No reference counterpart. */
+es_status es_submit_batch(es_engine *engine, const es_window *w, size_t n, uint64_t *ticket);
 
 es_status es_free_records(es_records *recs);
 

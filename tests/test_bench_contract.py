@@ -29,7 +29,15 @@ class StandInEngine:
         return {"short_max": 64, "rung_blocks_per_sm": 6, "long_split": 1}
 
     def run_batch(self, windows, schedule=1, records=True):
-        return [{"rung": 0} for _ in windows], None
+        import numpy as np
+        import es_sieve
+        return [{"rung": 0} for _ in windows], (np.zeros(3, dtype=es_sieve.RECORD_DTYPE) if records else None)
+
+    def submit_batch_c(self, warr, n):
+        return 1
+
+    def poll_c(self, ticket, carr, timeout_ms=-1):
+        return 1632
 
     def make_windows(self, windows):
         return windows
@@ -74,7 +82,8 @@ def test_gpu_arm_line_has_every_contract_key(monkeypatch, capsys):
     assert abs(line["value"] - line["config"]["integers_per_step"] / (TIMING["total_ms"] / 1000)) < 1
     for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
         assert k in line["e2e"], k
-    assert line["gpu_launches"] == 2 * TIMING["kernel_launches"]
+    assert "mode" in line["e2e"] and line["e2e_sync"]["value"] > 0
+    assert line["gpu_launches"] == 2 * 2 * TIMING["kernel_launches"]       # the synchronous and pipelined steps
     roof = line["roofline"]
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
         assert k in roof, k
@@ -82,6 +91,8 @@ def test_gpu_arm_line_has_every_contract_key(monkeypatch, capsys):
     assert 0 < roof["issue"]["frac"] < 2 and 0 < roof["stage_d"]["issue"]["frac"] < 2
     assert set(line["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}
     assert line["plain"]["records_identical"] and "c3" in line
+    b19 = line["batch19"]
+    assert b19["windows"] == 4096 and b19["value"] > 0 and b19["e2e"]["value"] > 0 and b19["plain"]["value"] > 0
     assert line["e2e_host_ms_per_step"]["total_ms"] == pytest.approx(TIMING["host_total_ms"])
 
 

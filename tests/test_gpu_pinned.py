@@ -68,6 +68,30 @@ def test_every_window_of_the_batch_matches_the_reference(name):
     assert sum(r[1] for r in rows) > 1000
 
 
+def test_pipelined_batches_match_the_reference():
+    """es_submit_batch with three batches in flight on the two serving streams (each batch's
+    marking chained after the previous one's, its stage D beside the next marking), the two
+    pinned batches alternating: every window of every batch still gives the reference's
+    SUMMARY and record digest."""
+    eng = engine()
+    names = ["batch4096", "batch19_4096"] * 3
+    data = {n: pinned(n) for n in set(names)}
+    tickets, done = [], []
+    for name in names:
+        tickets.append((name, eng.submit_batch(data[name][0])))
+        if len(tickets) >= 3:
+            n0, t0 = tickets.pop(0)
+            done.append((n0, eng.poll(t0, 4096, timeout_ms=120000)))
+    for n0, t0 in tickets:
+        done.append((n0, eng.poll(t0, 4096, timeout_ms=120000)))
+    assert [n for n, _ in done] == names
+    for name, (per, recs) in done:
+        wins, rows = data[name]
+        got = window_digests(eng, wins, per, recs)
+        bad = [i for i in range(len(wins)) if got[i] != rows[i]]
+        assert not bad, (name, bad[:5])
+
+
 def test_batch_fixture_windows_are_the_seeded_workloads():
     """The committed windows are what workloads.py draws on this machine (the bench reads the
     committed file, so a libm that rounds differently cannot change what is timed)."""
