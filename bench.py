@@ -38,14 +38,17 @@ import workloads  # noqa: E402
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 GPU_TABLE = os.path.join(GOLDEN, "filters", "f_M2042040_mmax2000_gpu.txt")
+# the filter table tuned for this engine (erdos-strauss_gb300/filter_tune.py; its own digest,
+# never the parity default): reported beside the reference's table
+GB300_TABLE = os.path.join(ROOT, "erdos-strauss_gb300", "tables", "f_M2042040_mmax2000_gb300.txt")
 METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
-# DRAM bytes (read + write) of one k_mark_short launch over the 4096-window batch: one ncu
-# capture of this kernel on this workload (dram__bytes_read.sum 79.56 MB +
-# dram__bytes_write.sum 2.44 MB); scaled by the algorithmic bytes when another batch size is run.
-MARK_SHORT_TRAFFIC_4096 = 79.559680e6 + 2.436608e6
-MARK_SHORT_ALG_4096 = 79280448               # the same launch's algorithmic bytes
-MARK_SHORT_INST_4096 = 823032516             # smsp__inst_executed.sum of the same capture
-RUNG_INST_4096 = 120287003                   # smsp__inst_executed.sum of one k_rung launch, same workload
+# One ncu capture per kernel schedule of the 4096-window batch with the gpu table (the
+# profiles/ summaries give the commands): per launch, the warp instructions
+# (smsp__inst_executed.sum) and DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum).
+# k_mark_short's depend on (short_max, long_split), k_rung's on rung_blocks_per_sm. A schedule
+# with no capture here gets no issue figure rather than another schedule's.
+MARK_SHORT_NCU = {}          # (short_max, long_split) -> {"inst": ..., "dram": ...}
+RUNG_NCU = {}                # rung_blocks_per_sm -> {"inst": ..., "dram": ...}
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
 MARKS_PER_INTEGER_GPU = 9.0951 / (2042040 / 2308)
@@ -61,10 +64,13 @@ def parse():
     ap.add_argument("--sieve", type=int, default=0, help="stage B' small primes up to P (rung_scan3 --sieve P)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-windows", type=int, default=CPU_WINDOWS,
+                    help="the CPU baseline's fixed sample: this many leading windows of the batch")
     ap.add_argument("--serve", type=int, default=2000, help="serving requests (0: no serving leg)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule")
+    ap.add_argument("--schedule", default="", help="short_max,rung_blocks_per_sm,long_split: set, no autotune")
     ap.add_argument("--no-batch19", action="store_true", help="skip the batch at [1e19, ceiling)")
+    ap.add_argument("--no-tuned-table", action="store_true", help="skip the legs with the GB300-tuned filter table")
     return ap.parse_args()
 
 
@@ -245,6 +251,41 @@ def l2_flusher(device):
         return (lambda: None), (lambda: None), "not flushed (%s)" % type(ex).__name__
 
 
+# The CPU baseline's fixed sample: the first CPU_WINDOWS windows of the batch (8.2e9 integers
+# of the seeded 4096-window batch), timed whole by both arms.
+CPU_WINDOWS = 256
+
+
+def host_cpu():
+    """The host's CPU model, instruction set and thread count (lscpu, else /proc/cpuinfo)."""
+    import platform
+    info = {"isa": platform.machine(), "threads": os.cpu_count(), "model": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            k, _, v = ln.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                info["model"] = v.strip()
+            if k.strip() == "Vendor ID" and v.strip():
+                info["vendor"] = v.strip()
+            if k.strip() == "Flags":
+                fl = v.split()
+                info["simd"] = [f for f in ("sse4_2", "avx2", "avx512f", "asimd", "sve", "sve2") if f in fl]
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            k, _, v = ln.partition(":")
+            if k.strip() == "Features" and "simd" not in info:
+                fl = v.split()
+                info["simd"] = [f for f in ("asimd", "sve", "sve2") if f in fl]
+            if k.strip() == "model name" and not info["model"]:
+                info["model"] = v.strip()
+    except OSError:
+        pass
+    return info
+
+
 def cpu_baseline(wins, seconds, threads=None):
     """The reference algorithm (CPU oracle port) on the host cores over the leading windows of
     the workload until `seconds` have elapsed. Returns (integers/s, windows done, cores)."""
@@ -270,14 +311,12 @@ def run_reference(args, ws, rank):
         return
     wins = workloads.batch_windows(args.windows)
     cores = os.cpu_count()
-    per_step = max(1, args.cpu_seconds / 3)
     for _ in range(args.warmup):
         cpu_baseline(wins[:2], 0.0, cores)
-    rates, tot_ints, tot_s, idx = [], 0, 0.0, 0
+    sample = wins[:args.cpu_windows]
+    tot_ints, tot_s = 0, 0.0
     for k in range(args.steps):
-        rate, done, _, el = cpu_baseline(wins[idx:], per_step, cores)
-        idx = (idx + done) % len(wins)
-        rates.append(rate)
+        rate, done, _, el = cpu_baseline(sample, float("inf"), cores)
         tot_ints += rate * el
         tot_s += el
     value = tot_ints / tot_s
@@ -287,8 +326,8 @@ def run_reference(args, ws, rank):
             "config": {"workload": "batch4096", "windows": args.windows, "wheel": 2042040,
                        "filters": "f_M2042040_mmax2000_gpu.txt", "seed": workloads.SEED},
             "cpu_baseline": {"value": value, "unit": "integers/s", "cores": cores, "kind": "port",
-                             "sample": "each step: consecutive windows of the 4096-window batch for ~%.0f s"
-                                       % per_step},
+                             "sample": "each step: the first %d windows of the 4096-window batch (%d integers)"
+                                       % (len(sample), integers(sample)), "host": host_cpu()},
             "e2e": {"value": value, "unit": "integers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -404,6 +443,93 @@ def pipelined_leg(eng, wins, steps, warmup, flush_async, depth=3):
     return run(steps)
 
 
+def roofline(args, wins, n_int, kern, stage, last_t, schedule, clocks):
+    """The dominant kernel against the bound that binds it. k_mark_short is instruction-issue
+    bound integer work: `achieved` is its warp instructions per launch (ncu, same schedule)
+    over its live CUDA-event time, `peak` 152 SMs x 4 schedulers x one instruction per cycle at
+    the sampled SM clock. Sub-objects: `hbm` (the kill-mask rows, stride residues and window
+    list one launch reads, over the same time, against the measured copy bandwidth), `marks`
+    (the per-mark view of a segment sieve) and `stage_d` (k_rung, latency-bound)."""
+    hbm_peak, peak_kind = peaks()
+    mhz = clocks.get("sm_mhz") or 2070.0
+    peak_issue = 152 * 4 * mhz * 1e6
+    per_kernel = {"k_mark_short": kern["mark_short_ms"], "k_mark": kern["mark_long_ms"], "k_prep": kern["prep_ms"],
+                  "k_mr": stage["mr_ms"], "k_rung": stage["rung_ms"], "k_direct": stage["direct_ms"]}
+    dom = max(per_kernel, key=per_kernel.get)
+    ms = per_kernel[dom] / args.steps
+    default = args.windows == 4096 and args.sieve == 0
+    cap = MARK_SHORT_NCU.get((schedule["short_max"], schedule["long_split"])) if default else None
+    if dom == "k_mark_short":
+        # one kill-mask row per lane (as laid out: the interleaved rounds padded), the per-window
+        # stride residues (u16 rows of 264) and the window list
+        alg = last_t["mask_bytes"] + len(wins) * 264 * 2 + len(wins) * 32
+    else:
+        alg = int(last_t["primes"]) * (24 + 64)             # the survivor tail: 24 B in, 64 B out per prime
+    roof = {"kernel": dom, "bound": "issue", "unit": "warp inst/s", "peak": peak_issue, "ms_per_launch": ms,
+            "achieved": None, "frac": None, "traffic": cap["dram"] if cap and dom == "k_mark_short" else None,
+            "schedule": schedule}
+    if cap and dom == "k_mark_short":
+        roof["achieved"] = cap["inst"] / (ms / 1000.0)
+        roof["frac"] = roof["achieved"] / peak_issue
+        roof["inst_per_launch"] = cap["inst"]
+    else:
+        roof["note"] = "no ncu capture for this kernel and schedule: no issue figure"
+    gbs = alg / (ms / 1000.0) / 1e9
+    roof["hbm"] = {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak, "peak_kind": peak_kind,
+                   "algorithmic_bytes": alg, "traffic": roof["traffic"]}
+    if dom == "k_mark_short" and args.sieve == 0:
+        # The per-mark view: a segment sieve clears one bit per mark with a 4-byte shared-memory
+        # read-modify-write (8 bytes); the kill-mask kernel does no per-mark work, so this is the
+        # bandwidth such a sieve would need to match it, against the nominal shared-memory rate
+        # (152 SMs x 128 B per cycle at the sampled clock).
+        marks = n_int * MARKS_PER_INTEGER_GPU
+        smem_peak = 152 * 128 * mhz * 1e6 / 1e9
+        rmw_gbs = marks * 8 / (ms / 1000.0) / 1e9
+        roof["marks"] = {"per_launch": marks, "achieved": marks / (ms / 1000.0), "unit": "marks/s",
+                         "rmw_equivalent_gbs": rmw_gbs, "smem_peak_gbs": smem_peak, "peak_kind": "nominal",
+                         "frac": rmw_gbs / smem_peak}
+    rcap = RUNG_NCU.get(schedule["rung_blocks_per_sm"]) if default else None
+    if stage["rung_ms"] > 0:
+        # The survivor tail (stage D): integer-pipe work bound by the latency of its hardest
+        # factorizations; the same issue arithmetic over k_rung's live time.
+        rung_ms = stage["rung_ms"] / args.steps
+        sd = {"kernel": "k_rung", "bound": "latency", "ms_per_launch": rung_ms, "issue": None}
+        if rcap:
+            rate = rcap["inst"] / (rung_ms / 1000.0)
+            sd["issue"] = {"achieved": rate, "peak": peak_issue, "unit": "warp inst/s", "frac": rate / peak_issue,
+                           "inst_per_launch": rcap["inst"]}
+        roof["stage_d"] = sd
+    return roof
+
+
+def tuned_table_leg(args, rank, local, schedule, flush, flush_async):
+    """Both batches with the GB300-tuned filter table instead of the reference's (same
+    schedule): device time of the kernels (synchronous calls, L2 flushed) and the pipelined
+    e2e, with the survivors and primes the table leaves."""
+    import hashlib
+    import es_sieve
+    body = "".join(ln for ln in open(GB300_TABLE) if ln.startswith("FILTER "))
+    out = {"table": os.path.basename(GB300_TABLE), "filters": body.count("\n"),
+           "sha256": hashlib.sha256(body.encode()).hexdigest()}
+    with es_sieve.Engine(wheel=2042040, filters=GB300_TABLE, device=local) as eng:
+        eng.set_schedule(short_max=schedule["short_max"], rung_blocks_per_sm=schedule["rung_blocks_per_sm"],
+                         long_split=schedule["long_split"])
+        for name, wins in (("batch4096", workloads.batch_windows(args.windows, seed=workloads.SEED + rank)),
+                           ("batch19", workloads.batch19_windows(args.windows, seed=workloads.SEED + rank))):
+            n = integers(wins)
+            for _ in range(args.warmup):
+                eng.run_batch(wins, records=False)
+            sy = sync_leg(eng, wins, args.steps, flush)
+            pw, _ = pipelined_leg(eng, wins, args.steps, args.warmup, flush_async)
+            out[name] = {"value": n * args.steps / (sy["dev_ms"] / 1000.0), "ms_per_step": sy["dev_ms"] / args.steps,
+                         "stages_ms_per_step": dict({k: v / args.steps for k, v in sy["stage"].items()},
+                                                    **{k: v / args.steps for k, v in sy["kern"].items()}),
+                         "survivors": int(sy["last"]["survivors"]), "primes": int(sy["last"]["primes"]),
+                         "e2e": {"value": n * args.steps / pw, "ms_per_step": 1000.0 * pw / args.steps,
+                                 "mode": "pipelined (es_submit_batch / es_poll, 3 in flight)"}}
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import es_sieve
     flush, flush_async, flush_note = l2_flusher(local)
@@ -411,7 +537,12 @@ def run_gpu(args, ws, rank, local):
     eng = es_sieve.Engine(wheel=2042040, filters=(mods, ress), device=local, sieve_p=args.sieve)
     wins = workloads.batch_windows(args.windows, seed=workloads.SEED + rank)
     n_int = integers(wins)
-    schedule = eng.autotune(wins, repeats=6) if not args.no_autotune else eng.schedule()
+    if args.schedule:
+        sm, rb, ls = (int(x) for x in args.schedule.split(","))
+        eng.set_schedule(short_max=sm, rung_blocks_per_sm=rb, long_split=ls)
+        schedule = eng.schedule()
+    else:
+        schedule = eng.autotune(wins, repeats=6) if not args.no_autotune else eng.schedule()
     for _ in range(args.warmup):
         eng.run_batch(wins)
     barrier(ws)
@@ -468,64 +599,30 @@ def run_gpu(args, ws, rank, local):
             b19["plain"] = {"value": n19 / (tp["total_ms"] / 1000.0), "ms_per_step": tp["total_ms"],
                             "kernel_launches": int(tp["kernel_launches"])}
         extra["batch19"] = b19
+    if not args.no_tuned_table and args.sieve == 0:
+        extra["gb300_table"] = tuned_table_leg(args, rank, local, schedule, flush, flush_async)
     if args.serve:
         serve_leg(eng, min(200, args.serve), workloads.SEED + 7)          # warm the serving slots
         extra["serve"] = serve_leg(eng, args.serve, workloads.SEED + 1000 * (rank + 1))
-    # roofline of the dominant kernel (per-kernel CUDA events on the engine's stream)
-    hbm, peak_kind = peaks()
-    per_kernel = {"k_mark_short": kern["mark_short_ms"], "k_mark": kern["mark_long_ms"], "k_prep": kern["prep_ms"],
-                  "k_mr": stage["mr_ms"], "k_rung": stage["rung_ms"], "k_direct": stage["direct_ms"]}
-    dom = max(per_kernel, key=per_kernel.get)
-    per_launch_ms = per_kernel[dom] / args.steps
-    if dom == "k_mark_short":
-        # one kill-mask row per lane from HBM, plus the per-window stride residues and window list
-        alg = last_t["mask_bytes"] + len(wins) * 263 * 2 + len(wins) * 32
-        traffic = MARK_SHORT_TRAFFIC_4096 * alg / MARK_SHORT_ALG_4096 if args.windows != 4096 else MARK_SHORT_TRAFFIC_4096
-    else:
-        # the survivor tail: 24 B in and 64 B out per prime
-        alg = int(last_t["primes"]) * (24 + 64)
-        traffic = None
-    achieved = alg / (per_launch_ms / 1000.0) / 1e9
-    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": traffic, "peak_kind": peak_kind, "algorithmic_bytes": alg, "ms_per_launch": per_launch_ms,
-            "note": "issue-bound integer work: the HBM fraction is small by construction"}
-    if dom == "k_mark_short" and args.windows == 4096:
-        # The bound that binds: instruction issue. Warp instructions of one launch (ncu
-        # smsp__inst_executed.sum on this workload) over the live launch time, against 152 SMs x 4
-        # schedulers x one instruction per cycle at the sampled SM clock.
-        inst = MARK_SHORT_INST_4096
-        mhz = clocks.get("sm_mhz") or 2070.0
-        peak_issue = 152 * 4 * mhz * 1e6
-        roof["issue"] = {"achieved": inst / (per_launch_ms / 1000.0), "peak": peak_issue, "unit": "warp inst/s",
-                         "frac": inst / (per_launch_ms / 1000.0) / peak_issue, "inst_per_launch": inst}
-    if dom == "k_mark_short" and args.sieve == 0:
-        # The per-mark view: a segment sieve clears one bit per mark with a 4-byte shared-memory
-        # read-modify-write (8 bytes); the kill-mask kernel does no per-mark work, so this is the
-        # bandwidth such a sieve would need to match it, against the nominal shared-memory rate
-        # (152 SMs x 128 B per cycle at the sampled clock).
-        marks = n_int * MARKS_PER_INTEGER_GPU
-        mhz = clocks.get("sm_mhz") or 2070.0
-        smem_peak = 152 * 128 * mhz * 1e6 / 1e9
-        rmw_gbs = marks * 8 / (per_launch_ms / 1000.0) / 1e9
-        roof["marks"] = {"per_launch": marks, "achieved": marks / (per_launch_ms / 1000.0), "unit": "marks/s",
-                         "rmw_equivalent_gbs": rmw_gbs, "smem_peak_gbs": smem_peak, "peak_kind": "nominal",
-                         "frac": rmw_gbs / smem_peak}
-    if args.windows == 4096 and args.sieve == 0 and stage["rung_ms"] > 0:
-        # The survivor tail (stage D): integer-pipe work bound by the latency of its hardest
-        # factorizations. Warp instructions of one k_rung launch (ncu smsp__inst_executed.sum on
-        # this workload) over its live time, against the same peak issue rate.
-        rung_launch_ms = stage["rung_ms"] / args.steps
-        mhz = clocks.get("sm_mhz") or 2070.0
-        peak_issue = 152 * 4 * mhz * 1e6
-        rate = RUNG_INST_4096 / (rung_launch_ms / 1000.0)
-        roof["stage_d"] = {"kernel": "k_rung", "bound": "latency", "ms_per_launch": rung_launch_ms,
-                           "issue": {"achieved": rate, "peak": peak_issue, "unit": "warp inst/s",
-                                     "frac": rate / peak_issue, "inst_per_launch": RUNG_INST_4096}}
+    roof = roofline(args, wins, n_int, kern, stage, last_t, schedule, clocks)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, done, cores, el = cpu_baseline(wins, args.cpu_seconds)
+        # the same fixed sample through both: the oracle port on every host thread, and the
+        # engine (device time of a synchronous es_run_batch, and its wall time from host buffers)
+        sample = wins[:args.cpu_windows]
+        rate, done, cores, el = cpu_baseline(sample, float("inf"))
+        for _ in range(2):
+            eng.run_batch(sample, records=False)
+        flush()
+        t0 = time.perf_counter()
+        eng.run_batch(sample)
+        wall_sample = time.perf_counter() - t0
+        ts = eng.timing()
         cpu = {"value": rate, "unit": "integers/s", "cores": cores, "kind": "port",
-               "sample": "first %d windows of the batch (%.1f s, all host threads)" % (done, el)}
+               "sample": "the first %d windows of the batch (%d integers, %.1f s, all host threads)"
+                         % (done, integers(sample), el), "host": host_cpu(),
+               "gpu_on_sample": {"value": integers(sample) / (ts["total_ms"] / 1000.0),
+                                 "e2e": integers(sample) / wall_sample, "mode": "es_run_batch"}}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "integers/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,

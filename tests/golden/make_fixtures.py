@@ -39,6 +39,10 @@ import workloads  # noqa: E402
 
 FILTERS = ["f_M120120_mmax2000_runtime.txt", "f_M2042040_mmax2000_gpu.txt", "f_M2042040_mmax2000_runtime.txt"]
 GPU = "f_M2042040_mmax2000_gpu.txt"
+# the table tuned for the GB300 engine (erdos-strauss_gb300/filter_tune.py): not the reference's,
+# so its fixtures are the reference's scanner run on it, never a copied golden
+GB300_TABLE = os.path.join(os.path.dirname(os.path.dirname(HERE)), "erdos-strauss_gb300", "tables",
+                           "f_M2042040_mmax2000_gb300.txt")
 
 
 def sha256(path):
@@ -85,7 +89,7 @@ def window_digests(sweep, wfile, table, out):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", nargs="*", default=["copied", "rows", "batch", "batch19"])
+    ap.add_argument("--only", nargs="*", default=["copied", "rows", "batch", "batch19", "gb300"])
     args = ap.parse_args()
     if not REF or not os.path.isdir(REF) or not os.path.exists(os.path.join(BIN, "rung_scan3")):
         raise SystemExit("set REF to the reference tree and build oracle/_ref (make -C oracle ref REF=...)")
@@ -163,8 +167,17 @@ def main():
         rows.append((name + ".windows", "workloads.%s" % wins.__name__, ["4096"]))
         window_digests(sweep, wf, F[GPU], os.path.join(gen, name + ".digests"))
         rows.append((name + ".digests", "ref_sweep", ["--windows", wf, "--filters", F[GPU]]))
+    if "gb300" in args.only:
+        # the tuned table through the reference's sweep_lane: the mid-height and top-of-range
+        # shards, and both batches window by window
+        for cfg in (workloads.c2(), workloads.c3()):
+            cli("%s_gb300.out" % cfg["name"], sweep, cfg["lo"], cfg["hi"], "--filters", GB300_TABLE)
+        for name in ("batch4096", "batch19_4096"):
+            wf = os.path.join(gen, name + ".windows")
+            window_digests(sweep, wf, GB300_TABLE, os.path.join(gen, name + "_gb300.digests"))
+            rows.append((name + "_gb300.digests", "ref_sweep", ["--windows", wf, "--filters", GB300_TABLE]))
     for name, binary, a in rows:
-        rel = [os.path.relpath(x, HERE) if x.startswith(HERE) else x for x in a]
+        rel = [os.path.relpath(x, HERE) if x.startswith(ROOT) else x for x in a]
         manifest["gen/" + name] = "%s %s %s" % (sha256(os.path.join(gen, name)), binary, " ".join(rel))
     for d in ("filters", "decades", "windows", "metas"):
         for name in sorted(os.listdir(os.path.join(HERE, d))):

@@ -57,6 +57,15 @@ class StandInEngine:
     def close(self):
         self.closed = True
 
+    def set_schedule(self, **kw):
+        pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
 
 def _bench(monkeypatch, argv):
     sys.path.insert(0, ROOT)
@@ -71,6 +80,9 @@ def _bench(monkeypatch, argv):
 
 def test_gpu_arm_line_has_every_contract_key(monkeypatch, capsys):
     bench = _bench(monkeypatch, ["--steps", "2", "--warmup", "3", "--serve", "0", "--no-cpu-baseline"])
+    # ncu figures for the stand-in's schedule only: the issue fraction must use them
+    monkeypatch.setattr(bench, "MARK_SHORT_NCU", {(64, 1): {"inst": 8e8, "dram": 82e6}})
+    monkeypatch.setattr(bench, "RUNG_NCU", {6: {"inst": 1.2e8, "dram": 1e6}})
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
@@ -87,17 +99,31 @@ def test_gpu_arm_line_has_every_contract_key(monkeypatch, capsys):
     roof = line["roofline"]
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
         assert k in roof, k
-    assert roof["kernel"] == "k_mark_short" and abs(roof["frac"] - roof["achieved"] / roof["peak"]) < 1e-12
-    assert 0 < roof["issue"]["frac"] < 2 and 0 < roof["stage_d"]["issue"]["frac"] < 2
+    assert roof["kernel"] == "k_mark_short" and roof["bound"] == "issue" and roof["unit"] == "warp inst/s"
+    assert abs(roof["frac"] - roof["achieved"] / roof["peak"]) < 1e-12 and 0 < roof["frac"] < 2
+    assert roof["traffic"] == 82e6 and roof["schedule"] == StandInEngine().schedule()
+    assert 0 < roof["hbm"]["frac"] < 1 and roof["hbm"]["unit"] == "GB/s"
+    assert 0 < roof["stage_d"]["issue"]["frac"] < 2
     assert set(line["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}
     assert line["plain"]["records_identical"] and "c3" in line
+    g = line["gb300_table"]
+    assert g["filters"] > 3745 and g["batch4096"]["value"] > 0 and g["batch19"]["e2e"]["value"] > 0
     b19 = line["batch19"]
     assert b19["windows"] == 4096 and b19["value"] > 0 and b19["e2e"]["value"] > 0 and b19["plain"]["value"] > 0
     assert line["e2e_host_ms_per_step"]["total_ms"] == pytest.approx(TIMING["host_total_ms"])
 
 
+def test_roofline_without_a_capture_for_the_schedule(monkeypatch, capsys):
+    bench = _bench(monkeypatch, ["--steps", "1", "--warmup", "3", "--serve", "0", "--no-cpu-baseline", "--no-plain",
+                                 "--no-batch19"])
+    monkeypatch.setattr(bench, "MARK_SHORT_NCU", {(128, 1): {"inst": 8e8, "dram": 82e6}})
+    bench.main()
+    roof = json.loads(capsys.readouterr().out.strip().splitlines()[-1])["roofline"]
+    assert roof["achieved"] is None and roof["frac"] is None and "note" in roof
+
+
 def test_reference_arm_line(monkeypatch, capsys):
-    bench = _bench(monkeypatch, ["--impl", "reference", "--steps", "1", "--warmup", "1", "--cpu-seconds", "0.3"])
+    bench = _bench(monkeypatch, ["--impl", "reference", "--steps", "1", "--warmup", "1", "--cpu-windows", "3"])
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0

@@ -68,7 +68,7 @@ def test_reference_arm_rank_other_than_zero_does_no_work(monkeypatch):
     import bench
 
     class A:
-        windows, warmup, steps, cpu_seconds = 4, 0, 1, 0.1
+        windows, warmup, steps, cpu_windows = 4, 0, 1, 2
     called = []
     monkeypatch.setattr(bench, "cpu_baseline", lambda *a, **k: called.append(1))
     bench.run_reference(A(), 2, 1)
