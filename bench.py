@@ -47,8 +47,16 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # (smsp__inst_executed.sum) and DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum).
 # k_mark_short's depend on (short_max, long_split), k_rung's on rung_blocks_per_sm. A schedule
 # with no capture here gets no issue figure rather than another schedule's.
-MARK_SHORT_NCU = {}          # (short_max, long_split) -> {"inst": ..., "dram": ...}
-RUNG_NCU = {}                # rung_blocks_per_sm -> {"inst": ..., "dram": ...}
+MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
+    (32, 1): {"inst": 945565966, "dram": 95801856 + 3509760},
+    (64, 1): {"inst": 872798519, "dram": 95262208 + 3462144},
+    (128, 1): {"inst": 877197944, "dram": 95223808 + 3796224},
+}
+RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
+    4: {"inst": 82244672, "dram": 854784},
+    6: {"inst": 82512744, "dram": 858112 + 256},
+    8: {"inst": 82600016, "dram": 846592},
+}
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
 MARKS_PER_INTEGER_GPU = 9.0951 / (2042040 / 2308)
@@ -70,6 +78,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule")
     ap.add_argument("--schedule", default="", help="short_max,rung_blocks_per_sm,long_split: set, no autotune")
     ap.add_argument("--no-batch19", action="store_true", help="skip the batch at [1e19, ceiling)")
+    ap.add_argument("--no-pipelined", action="store_true",
+                    help="skip the pipelined leg (for profiler runs: under ncu the process ended with a "
+                         "segmentation fault when the pipelined leg started); e2e is then the synchronous figure")
     ap.add_argument("--no-tuned-table", action="store_true", help="skip the legs with the GB300-tuned filter table")
     return ap.parse_args()
 
@@ -548,7 +559,10 @@ def run_gpu(args, ws, rank, local):
     barrier(ws)
     with Clocks(local) as clk:
         sy = sync_leg(eng, wins, args.steps, flush)
-        pipe_wall, pipe_recs = pipelined_leg(eng, wins, args.steps, args.warmup, flush_async)
+        if args.no_pipelined:
+            pipe_wall, pipe_recs = sy["wall_s"], sy["recs"]
+        else:
+            pipe_wall, pipe_recs = pipelined_leg(eng, wins, args.steps, args.warmup, flush_async)
     barrier(ws)
     clocks = clk.summary()
     dev_ms, wall_s, launches, recs_n = sy["dev_ms"], sy["wall_s"], sy["launches"], sy["recs"]
@@ -637,13 +651,15 @@ def run_gpu(args, ws, rank, local):
                 # graph copies the first 4096 record slots back every run, any more afterwards)
                 "e2e": {"value": e2e, "unit": "integers/s", "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),
                         "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * max(pipe_recs, 4096),
-                        "mode": "pipelined: es_submit_batch / es_poll, 3 batches in flight, host buffers in and out",
+                        "mode": ("es_run_batch, one call per step" if args.no_pipelined else
+                                 "pipelined: es_submit_batch / es_poll, 3 batches in flight, host buffers in and out"),
                         "ms_per_step": 1000.0 * pipe / args.steps},
                 "e2e_sync": {"value": e2e_sync, "unit": "integers/s", "mode": "es_run_batch, one call per step",
                              "h2d_bytes_per_step": 16 + len(wins) * (48 + 32),
                              "d2h_bytes_per_step": 68 + 64 * len(wins) + 64 * max(recs_n, 4096),
                              "ms_per_step": 1000.0 * wall / args.steps},
-                "gpu_launches": launches + int(last_t["kernel_launches"]) * args.steps, "clocks": clocks,
+                "gpu_launches": launches + (0 if args.no_pipelined else int(last_t["kernel_launches"]) * args.steps),
+                "clocks": clocks,
                 "roofline": roof, "cpu_baseline": cpu,
                 "stages_ms_per_step": dict({k: v / args.steps for k, v in stage.items()},
                                            **{k: v / args.steps for k, v in kern.items()}),

@@ -66,6 +66,23 @@ def test_parse_production_meta():
     assert d["table_sha256"].startswith("6af5e762")
 
 
+def test_shard_0_rederived_on_gb300_matches_production():
+    """Shard 0 of the reference's 250-shard run over [255255, 10^19) (data/c19/shard_0.meta, an
+    L4 run), re-derived on one GB300 by the drop-in binary (its command and wall time are in the
+    meta's header): the same certificate count, the same sha256 of the 394 M certificate lines in
+    the same order, the same SUMMARY, the same filter table."""
+    path = golden("metas", "gb300_shard_0.meta")
+    if not os.path.exists(path):
+        pytest.skip("no GB300 re-derivation of shard 0 committed")
+    ref = shard_meta.parse_meta(read("metas", "c19_shard_0.meta"))
+    got = shard_meta.parse_meta(open(path).read())
+    assert got["complete"] and got["idx"] == 0 and got["nshards"] == 250 and got["rc"] == 0
+    assert shard_meta.audit(ref, got) == []
+    for k in ("certs", "cert_sha256", "lo", "hi", "positions", "covered", "mr", "composite", "rung", "direct",
+              "survivors", "table_sha256"):
+        assert got[k] == ref[k], k
+
+
 def test_audit():
     a = shard_meta.parse_meta(read("metas", "c19_shard_0.meta"))
     assert shard_meta.audit(a, dict(a)) == []
