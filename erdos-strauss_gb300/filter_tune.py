@@ -247,9 +247,10 @@ def segment_histogram(windows, M, nlanes, short_max=64):
     return hist
 
 
-def prefix_table(rank, order, primes_mask, zs, nrounds_cap=None):
+def prefix_table(rank, order, primes_mask, zs):
     """Per prefix k (1..len(order)) and segment size z: survivors and primes per position,
-    and rounds per task, from the domain's ranks."""
+    and rounds per task, from the domain's ranks (primes counted for the prefixes no shorter
+    than the one primes_mask was made for)."""
     L, npos = rank.shape
     n = len(order)
     ks = np.arange(1, n + 1)
