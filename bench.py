@@ -53,9 +53,9 @@ MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
     (128, 1): {"inst": 877197944, "dram": 95223808 + 3796224},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
-    4: {"inst": 82244672, "dram": 854784},
-    6: {"inst": 82512744, "dram": 858112 + 256},
-    8: {"inst": 82600016, "dram": 846592},
+    4: {"inst": 79777982, "dram": 812288 + 256},
+    6: {"inst": 80175159, "dram": 816896},
+    8: {"inst": 80002415, "dram": 816384},
 }
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.

@@ -19,16 +19,19 @@
 // Curves: Montgomery form B y^2 = x^3 + A x^2 + x with Suyama's parametrization (sigma ->
 // u = sigma^2 - 5, v = 4 sigma, starting point (u^3 : v^3), (A + 2)/4 = (v - u)^3 (3u + v) /
 // (16 u^3 v)), whose group orders are divisible by 12. x-only arithmetic in projective
-// coordinates (Montgomery 1987): doubling and differential addition. Stage 1 multiplies by
-// k = product of the largest powers of the primes p <= B1 that are <= B1, with the ladder;
-// stage 2 is the standard baby-step giant-step continuation with D = 60: for every prime q in
-// (B1, B2], written q = mD +- j with j coprime to 60, the product accumulates
-// X([mD]Q) Z([j]Q) - X([j]Q) Z([mD]Q), with the baby steps normalised to Z = 1.
+// coordinates (Montgomery 1987): doubling and differential addition, with (A + 2)/4 kept as
+// a fraction, so that a curve takes no modular inverse at all (an inverse -- a data-dependent
+// binary extended Euclid -- cost about as much as a quarter of a curve here). Stage 1
+// multiplies by k = product of the largest powers of the primes p <= B1 that are <= B1, with
+// the ladder; stage 2 is the standard baby-step giant-step continuation with D = 60: for every
+// prime q in (B1, B2], written q = mD +- j with j coprime to 60, the product accumulates
+// X([mD]Q) Z([j]Q) - X([j]Q) Z([mD]Q), and one gcd with n at the end finds the factor.
 //
 // Everything here is modular arithmetic modulo n in Montgomery form (the lazy representation of
-// es_arith.cuh for n < 2^62); a divisor comes only out of gcd(., n), so it always divides n. All lanes of a warp run the same sequence of
-// curve operations (k and the stage-2 table are the same for every lane), so the warp stays
-// converged apart from the short gcd and inverse loops. Every loop is bounded.
+// es_arith.cuh for n < 2^62); a divisor comes only out of gcd(., n), so it always divides n.
+// All lanes of a warp run the same sequence of curve operations (k and the stage-2 table are
+// the same for every lane), so the warp stays converged apart from the final gcd. Every loop
+// is bounded.
 #pragma once
 #include "es_arith.cuh"
 
@@ -50,41 +53,23 @@ __constant__ const unsigned char ECM_PAIRS[ECM_M1] = {
     0xff, 0xfe, 0xff, 0xdf, 0xfe, 0xef, 0xed, 0xff, 0xf3, 0xfb, 0xfb, 0xef, 0xf6, 0xfd, 0xfe, 0x7e,
     0xef, 0xfe, 0x5c, 0xfb, 0xf5, 0xfb, 0xab, 0x3f, 0xff, 0xf7, 0x7f, 0xfc, 0x3b, 0x5d, 0xbf, 0xae,
     0xbb};
-// One round (about 1.3 K Montgomery multiplies: 10 per bit of k, 2 per stage-2 pair, 6 per
+// One round (about 1.6 K Montgomery multiplies: 12 per bit of k, 3 per stage-2 pair, 6 per
 // giant step) in rho steps of two multiplies.
-constexpr u64 ECM_ROUND_STEPS = 700;
-
-__device__ __forceinline__ u64 submod(u64 a, u64 b, u64 n) {   // a, b < n
-  return a >= b ? a - b : a + (n - b);
-}
-
-// a^-1 mod n for odd n > 1 and gcd(a, n) = 1, 0 < a < n (binary extended Euclid: x1 a = u and
-// x2 a = v mod n throughout). Every pass of the outer loop halves u or v at least once, so it
-// ends within 128 passes; the bound only guards the invariant. Returns 0 if it is hit.
-__device__ inline u64 inv_mod(u64 a, u64 n) {
-  u64 u = a, v = n, x1 = 1, x2 = 0;
-  for (int guard = 0; guard < 256; ++guard) {
-    if (u == 1) return x1;
-    if (v == 1) return x2;
-    while (!(u & 1)) { u >>= 1; x1 = (x1 & 1) ? (x1 >> 1) + (n >> 1) + 1 : x1 >> 1; }
-    while (!(v & 1)) { v >>= 1; x2 = (x2 & 1) ? (x2 >> 1) + (n >> 1) + 1 : x2 >> 1; }
-    if (u >= v) { u -= v; x1 = submod(x1, x2, n); }
-    else { v -= u; x2 = submod(x2, x1, n); }
-    if (u == 0 || v == 0) return 0;                  // gcd(a, n) > 1: not invertible
-  }
-  return 0;
-}
+constexpr u64 ECM_ROUND_STEPS = 800;
 
 struct XZ { u64 x, z; };
 
 // The curve operations over an arithmetic policy Ar (ExactArith or LazyArith, es_arith.cuh).
-// [2]P; a24 = (A + 2)/4.
+// [2]P with (A + 2)/4 = a24n / a24d: X = t1 t2, Z = t3 (t2 + a24 t3) (t1 = (x + z)^2,
+// t2 = (x - z)^2, t3 = t1 - t2) with both coordinates multiplied by a24d, so that no inverse
+// of a24d is needed.
 template <class Ar>
-__device__ __forceinline__ XZ ecm_dbl(XZ P, u64 a24, const Mont &M) {
+__device__ __forceinline__ XZ ecm_dbl(XZ P, u64 a24n, u64 a24d, const Mont &M) {
   const u64 s = Ar::add(P.x, P.z, M), d = Ar::sub(P.x, P.z, M);
   const u64 t1 = Ar::mul(s, s, M), t2 = Ar::mul(d, d, M);
   const u64 t3 = Ar::sub(t1, t2, M);                           // 4xz
-  return XZ{Ar::mul(t1, t2, M), Ar::mul(t3, Ar::add(t2, Ar::mul(a24, t3, M), M), M)};
+  const u64 c = Ar::mul(a24d, t2, M);
+  return XZ{Ar::mul(t1, c, M), Ar::mul(t3, Ar::add(c, Ar::mul(a24n, t3, M), M), M)};
 }
 // P + Q given D = P - Q.
 template <class Ar>
@@ -94,23 +79,7 @@ __device__ __forceinline__ XZ ecm_add(XZ P, XZ Q, XZ D, const Mont &M) {
   const u64 s = Ar::add(u, v, M), d = Ar::sub(u, v, M);
   return XZ{Ar::mul(D.z, Ar::mul(s, s, M), M), Ar::mul(D.x, Ar::mul(d, d, M), M)};
 }
-// P + Q given P - Q = (dx : 1).
-template <class Ar>
-__device__ __forceinline__ XZ ecm_add1(XZ P, XZ Q, u64 dx, const Mont &M) {
-  const u64 u = Ar::mul(Ar::sub(P.x, P.z, M), Ar::add(Q.x, Q.z, M), M);
-  const u64 v = Ar::mul(Ar::add(P.x, P.z, M), Ar::sub(Q.x, Q.z, M), M);
-  const u64 s = Ar::add(u, v, M), d = Ar::sub(u, v, M);
-  return XZ{Ar::mul(s, s, M), Ar::mul(dx, Ar::mul(d, d, M), M)};
-}
 
-// Montgomery form of w^-1 for a Montgomery residue w (w = W 2^64 mod n, any representative):
-// 0 if not invertible.
-template <class Ar>
-__device__ __forceinline__ u64 mont_inverse(u64 w, const Mont &M) {
-  const u64 t = inv_mod(Ar::norm(w, M), M.n);                  // W^-1 2^-64
-  if (!t) return 0;
-  return Ar::mul(Ar::mul(t, M.r2, M), M.r2, M);                // W^-1, then W^-1 2^64
-}
 
 // Divisor d of n from gcd(g, n), if it is a proper one; else 0.
 __device__ __forceinline__ u64 proper_gcd(u64 g, u64 n) {
@@ -135,9 +104,9 @@ constexpr int ECM_STAGE1_POLL = ES_ECM_STAGE1_POLL;
 template <class Ar, class Poll>
 __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
   const u64 n = M.n;
-  u64 found = 0;
-  bool dead = false;
-  // --- the curve and its starting point
+  // --- the curve and its starting point, kept projective: (A + 2)/4 = num / den and the point
+  // (u^3 : v^3), so that no inverse is taken (a curve that is degenerate modulo a factor of n
+  // only makes the final gcd find that factor, or fail)
   const u64 sm = to_mont(sigma, M);
   const u64 five = to_mont(5, M);
   const u64 u = Ar::sub(Ar::mul(sm, sm, M), five, M);
@@ -148,34 +117,22 @@ __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
   u64 den = Ar::mul(u3, v, M);
   #pragma unroll
   for (int i = 0; i < 4; ++i) den = Ar::add(den, den, M);      // 16 u^3 v
-  const u64 w = Ar::mul(den, v3, M);
-  u64 winv = 0;
-  {
-    const u64 g = gcd64(w, n);
-    if (g != 1) { dead = true; if (g < n) found = g; }
-    else winv = mont_inverse<Ar>(w, M);
-    if (!winv) dead = true;
-  }
-  const u64 x = Ar::mul(Ar::mul(u3, den, M), winv, M);         // u^3 / v^3
-  const u64 a24 = Ar::mul(Ar::mul(num, v3, M), winv, M);       // (A + 2) / 4
-  // --- stage 1: Q = [k](x : 1), ladder from the top bit of k
-  XZ R0{x, M.one}, R1 = ecm_dbl<Ar>(R0, a24, M);
+  const XZ P0{u3, v3};
+  // --- stage 1: Q = [k]P0, ladder from the top bit of k (the difference of the ladder's two
+  // points is always P0)
+  XZ R0 = P0, R1 = ecm_dbl<Ar>(R0, num, den, M);
   for (int i = ECM_K_BITS - 2; i >= 0; --i) {
     const bool b = (ECM_K[i >> 5] >> (i & 31)) & 1u;
     if (b) { const XZ t = R0; R0 = R1; R1 = t; }
-    R1 = ecm_add1<Ar>(R0, R1, x, M);
-    R0 = ecm_dbl<Ar>(R0, a24, M);
+    R1 = ecm_add<Ar>(R0, R1, P0, M);
+    R0 = ecm_dbl<Ar>(R0, num, den, M);
     if (b) { const XZ t = R0; R0 = R1; R1 = t; }
     if (i && i % ECM_STAGE1_POLL == 0 && poll()) return 0;
   }
   const XZ Q = R0;
-  if (!dead) {
-    const u64 g = gcd64(Q.z, n);
-    if (g != 1) { dead = true; if (g < n) found = g; }
-  }
   if (poll()) return 0;
   // --- stage 2: baby steps [j]Q for odd j <= 31 (kept for j in ECM_J), giant step [60]Q
-  const XZ Q2 = ecm_dbl<Ar>(Q, a24, M);
+  const XZ Q2 = ecm_dbl<Ar>(Q, num, den, M);
   u64 bx[ECM_NJ], bz[ECM_NJ];
   bx[0] = Q.x; bz[0] = Q.z;
   XZ prev = Q, cur = ecm_add<Ar>(Q2, Q, Q, M);                 // [1], [3]
@@ -189,38 +146,20 @@ __device__ inline u64 ecm_curve(u64 sigma, const Mont &M, Poll poll) {
     prev = cur; cur = nxt;
   }
   const XZ G1 = ecm_add<Ar>(cur, P29, Q2, M);                  // [31] + [29] = [60]
-  // normalise the baby steps: xn[i] = X_j / Z_j (one inverse for all eight)
-  u64 c[ECM_NJ];
-  c[0] = bz[0];
-  #pragma unroll
-  for (int i = 1; i < ECM_NJ; ++i) c[i] = Ar::mul(c[i - 1], bz[i], M);
-  u64 inv = 0;
-  if (!dead) {
-    const u64 g = gcd64(c[ECM_NJ - 1], n);
-    if (g != 1) { dead = true; if (g < n) found = g; }
-    else { inv = mont_inverse<Ar>(c[ECM_NJ - 1], M); if (!inv) dead = true; }
-  }
-  u64 xn[ECM_NJ];
-  #pragma unroll
-  for (int i = ECM_NJ - 1; i > 0; --i) {
-    xn[i] = Ar::mul(bx[i], Ar::mul(inv, c[i - 1], M), M);
-    inv = Ar::mul(inv, bz[i], M);
-  }
-  xn[0] = Ar::mul(bx[0], inv, M);
-  // giant steps G_m = [60 m]Q, m = 1 .. ECM_M1
-  u64 acc = M.one;
+  // giant steps G_m = [60 m]Q, m = 1 .. ECM_M1; for each prime mD +- j of (B1, B2] the
+  // product gathers X(G_m) Z(j) - X(j) Z(G_m), zero modulo p when [mD]Q = +-[j]Q there. It
+  // starts from Z(Q): a factor stage 1 already found (Q at infinity modulo p) stays in it.
+  u64 acc = Q.z;
   XZ Gp = G1, G = G1;
   for (int m = 1; m <= ECM_M1; ++m) {
-    if (m == 2) G = ecm_dbl<Ar>(G1, a24, M);
+    if (m == 2) G = ecm_dbl<Ar>(G1, num, den, M);
     else if (m > 2) { const XZ t = ecm_add<Ar>(G, G1, Gp, M); Gp = G; G = t; }
     const u32 mask = ECM_PAIRS[m - 1];
     #pragma unroll
     for (int i = 0; i < ECM_NJ; ++i)
-      if (mask & (1u << i)) acc = Ar::mul(acc, Ar::sub(G.x, Ar::mul(xn[i], G.z, M), M), M);
+      if (mask & (1u << i)) acc = Ar::mul(acc, Ar::sub(Ar::mul(G.x, bz[i], M), Ar::mul(bx[i], G.z, M), M), M);
     if (m % ECM_STAGE2_POLL == 0 && poll()) return 0;
   }
-  if (!dead) found = proper_gcd(acc, n);
-  return found;
+  return proper_gcd(Ar::norm(acc, M), n);
 }
-
 }  // namespace es

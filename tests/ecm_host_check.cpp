@@ -1,10 +1,11 @@
 // Host build of the device ECM (erdos-strauss_gb300/csrc/es_ecm.cuh) for the CPU tests: the
 // same source compiled by g++ with the four device intrinsics it uses defined on 128-bit host
-// integers. Checks the binary inverse on random residues, the lazy Montgomery multiply against
-// exact residues and the lazy strong-probable-prime round against the exact one, then runs 32 curves (sigma 6..37, one warp's first round) on seeded
-// 62-bit semiprimes with prime factors of 18-31 bits in the lazy arithmetic the engine uses
-// and prints the fraction of curves that split each size; the exact arithmetic must find the
-// same divisors curve for curve, and every divisor returned must divide n properly.
+// integers. Checks the lazy Montgomery multiply against exact residues and the lazy
+// strong-probable-prime round against the exact one, then runs 32 curves (sigma 6..37, one
+// warp's first round) on seeded 62-bit semiprimes with prime factors of 18-31 bits in the lazy
+// arithmetic the engine uses and prints the fraction of curves that split each size; the exact
+// arithmetic must find the same divisors curve for curve, and every divisor returned must
+// divide n properly.
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -47,15 +48,6 @@ static u64 random_prime(int bits, std::mt19937_64 &g) {
 int main(int argc, char **argv) {
   const int trials = argc > 1 ? atoi(argv[1]) : 40;
   std::mt19937_64 g(0xE52026);
-  for (int t = 0; t < 20000; ++t) {
-    const u64 n = g() | 1, a = g() % n;
-    if (n < 3 || !a) continue;
-    const u64 x = inv_mod(a, n);
-    if (gcd64(a, n) == 1 ? (unsigned __int128)a * x % n != 1 : x != 0) {
-      printf("FAIL inverse a=%llu n=%llu\n", a, n);
-      return 1;
-    }
-  }
   for (int t = 0; t < 200000; ++t) {
     const u64 n = (g() >> 2) | 1;
     if (n < 3) continue;
