@@ -389,6 +389,7 @@ def main():
     ap.add_argument("--out", default=".")
     ap.add_argument("--calibrate", default="", help="JSON of measured batch timings per prefix")
     ap.add_argument("--measure", default="", help="time the --prefixes tables on the GPU, write this JSON")
+    ap.add_argument("--measure-steps", type=int, default=10, help="timed calls per table for --measure")
     ap.add_argument("--write", default="", help="write the tuned table here")
     ap.add_argument("--report", action="store_true")
     ap.add_argument("--compare", default="", help="a filter table file to report on the same domains")
@@ -435,7 +436,7 @@ def main():
         written.append((k, path))
         print(path, digest)
     if args.measure:
-        measure([p for _, p in written], [k for k, _ in written], args.measure)
+        measure([p for _, p in written], [k for k, _ in written], args.measure, args.measure_steps)
     if args.calibrate:
         # [{"k": k, "mark_short_ms": .., "mr_ms": .., "rung_ms": ..}, ...] of one batch per prefix
         meas = json.load(open(args.calibrate))

@@ -45,3 +45,23 @@ def test_every_window_of_the_batch_matches_the_reference(name):
         got = window_digests(eng, wins, per, recs)
         bad = [i for i in range(len(wins)) if got[i] != rows[i]]
         assert not bad, (sched, bad[:5])
+
+
+def test_tuner_measures_prefix_tables_on_the_gpu(tmp_path):
+    """filter_tune.py --measure: two prefix tables through the engine, one timed call each;
+    the calibration file it writes holds the per-kernel times and the counts the fit reads, and
+    the longer prefix leaves fewer survivors."""
+    import json
+    import subprocess
+    import sys
+    out = tmp_path / "cal.json"
+    r = subprocess.run([sys.executable, os.path.join(PKG, "filter_tune.py"), "--prefixes", "96,160", "--out",
+                        str(tmp_path), "--measure", str(out), "--measure-steps", "1"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rows = json.load(open(out))["rows"]
+    assert [row["k"] for row in rows] == [96, 160]
+    for row in rows:
+        assert row["mark_short_ms"] > 0 and row["mr_ms"] > 0 and row["rung_ms"] > 0
+    assert rows[1]["survivors"] < rows[0]["survivors"] and rows[1]["primes"] < rows[0]["primes"]
+
