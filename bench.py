@@ -48,14 +48,14 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # k_mark_short's depend on (short_max, long_split), k_rung's on rung_blocks_per_sm. A schedule
 # with no capture here gets no issue figure rather than another schedule's.
 MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
-    (32, 1): {"inst": 945565966, "dram": 95801856 + 3509760},
-    (64, 1): {"inst": 872798519, "dram": 95262208 + 3462144},
-    (128, 1): {"inst": 877197944, "dram": 95223808 + 3796224},
+    (32, 1): {"inst": 826632339, "dram": 95779584 + 3481344},
+    (64, 1): {"inst": 768759852, "dram": 95262720 + 3449344},
+    (128, 1): {"inst": 784637251, "dram": 94985984 + 3377920},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
-    4: {"inst": 79777982, "dram": 812288 + 256},
-    6: {"inst": 80175159, "dram": 816896},
-    8: {"inst": 80002415, "dram": 816384},
+    4: {"inst": 79067229, "dram": 814592},
+    6: {"inst": 79324859, "dram": 808448},
+    8: {"inst": 79292614, "dram": 817152},
 }
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.

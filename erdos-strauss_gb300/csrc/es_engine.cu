@@ -293,6 +293,16 @@ __global__ void __launch_bounds__(BLOCK) k_mark(const MarkParams P, int persiste
 #define ES_SHORT_LANES 2
 #endif
 constexpr int SHORT_LANES = ES_SHORT_LANES;
+// Windows with at most SPARSE_N positions in either lane of a k_mark_short CTA take the sparse
+// first round (short_sparse_round). Measured on the 4096-window batch: 0.87 ms for the kernel
+// with 32, 0.98 without the sparse round, 0.88 with 16, 0.93 with 48 or 64 (a second chunk
+// per lane: the task path marks those windows for less).
+#ifndef ES_SPARSE_N
+#define ES_SPARSE_N 32
+#endif
+constexpr u32 SPARSE_N = ES_SPARSE_N;
+static_assert(SPARSE_N <= 32, "a sparse window's positions fit one 32-position chunk per lane");
+constexpr u32 HAND_WORDS = SHORT_LANES;          // alive words per window handed on, one per lane
 constexpr u32 SMD_MAX = 512;       // stride descriptors staged in shared memory
 
 
@@ -456,19 +466,30 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
                                                const MaskDesc *smd, u32 l_first, const WinRef &R,
                                                const u64 (&rho)[SHORT_LANES], const u32 (&n)[SHORT_LANES],
                                                const u32 (&b)[SHORT_LANES], const u16 *const (&K0row)[SHORT_LANES],
-                                               u32 q0_first, u32 lane, const MaskDesc &md0) {
+                                               u32 q0_first, u32 lane, const MaskDesc &md0, const u32 *hand_j) {
   const u32 wi = R.wi;
   const u16 *Qrow = P.Qm + (size_t)wi * P.Dq;
   u32 alive[SHORT_LANES][NC];
-  #pragma unroll
-  for (int q = 0; q < SHORT_LANES; ++q)
+  u32 cnt;
+  if (NC == 1 && hand_j) {                         // the sparse round did the first round
     #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const u32 lo = 32 * c;
-      alive[q][c] = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
-    }
-  u32 cnt = short_phase<NC>(alive, P, tab, tab_words, smd, 0, P.nm_cov, 0, P.nl_cov, n, b, K0row, Qrow, q0_first,
-                            lane, md0);
+    for (int q = 0; q < SHORT_LANES; ++q) alive[q][0] = hand_j[q];
+    const u32 k = 32 + lane;
+    const MaskDesc md1 = k < P.nm_cov ? smd[k] : MaskDesc{1, 0, 0, 0};
+    const u32 q1 = k < P.nm_cov ? (u32)__ldg(Qrow + md1.d) : 0u;
+    cnt = short_phase<NC>(alive, P, tab, tab_words, smd, min(32u, P.nm_cov), P.nm_cov, 0, P.nl_cov, n, b, K0row,
+                          Qrow, q1, lane, md1);
+  } else {
+    #pragma unroll
+    for (int q = 0; q < SHORT_LANES; ++q)
+      #pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const u32 lo = 32 * c;
+        alive[q][c] = n[q] >= lo + 32 ? ~0u : (n[q] > lo ? (1u << (n[q] - lo)) - 1 : 0u);
+      }
+    cnt = short_phase<NC>(alive, P, tab, tab_words, smd, 0, P.nm_cov, 0, P.nl_cov, n, b, K0row, Qrow, q0_first,
+                          lane, md0);
+  }
   if (cnt && (P.nm_all > P.nm_cov || P.nl_all > P.nl_cov)) {          // stage B'
     if (lane == 0) atomicAdd(&P.cnt[wi].after_covers, (unsigned long long)cnt);
     const u32 k = P.nm_cov + lane;
@@ -507,6 +528,52 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
   }
 }
 
+// The sparse windows of a 32-window group (at most SPARSE_N positions in either lane of the
+// CTA: windows shorter than a few wheel periods) get the first round of strides alone, window
+// after window with the next window's residue loaded ahead: lane k extracts the kill word of
+// stride k for both lanes' positions, one warp OR each, and nothing else -- no task set-up.
+// The first round kills all but ~1% of positions, so almost every sparse window ends there;
+// the few with a position still alive are returned as a mask of the group's lanes, their alive
+// words left in hand[window][lane], and the task path goes on with them from the second round.
+// Counters and survivors are the task path's alone.
+
+__device__ __forceinline__ unsigned short_sparse_round(const ShortParams &P, const u32 *tab, u32 tab_words,
+                                                       const MaskDesc &md0, u32 xwi, u32 pk, unsigned sp,
+                                                       u32 *hand, u32 lane) {
+  static_assert(SHORT_LANES == 2, "two lanes per CTA");
+  const bool has = lane < P.nm_cov;                // lane k holds the first round's stride k
+  auto ldq = [&](u32 wi) { return has ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + md0.d) : 0u; };
+  unsigned again = 0;
+  u32 qn = ldq(__shfl_sync(FULL, xwi, __ffs(sp) - 1));
+  while (sp) {
+    const int j = __ffs(sp) - 1;
+    sp &= sp - 1;
+    const u32 pj = __shfl_sync(FULL, pk, j);
+    const u32 qd = qn;
+    if (sp) qn = ldq(__shfl_sync(FULL, xwi, __ffs(sp) - 1));
+    u32 kill0 = 0, kill1 = 0;
+    if (has) {
+      u32 r = qd + ((pj >> 24) & 1u);
+      r = r >= md0.s ? r - md0.s : r;
+      const u32 *wp = tab + md0.off + ((r >> 5) << md0.sh);
+      kill0 = __funnelshift_r(wp[0], wp[1u << md0.sh], r & 31);
+      r = qd + ((pj >> 25) & 1u);
+      r = r >= md0.s ? r - md0.s : r;
+      wp = tab + tab_words + md0.off + ((r >> 5) << md0.sh);
+      kill1 = __funnelshift_r(wp[0], wp[1u << md0.sh], r & 31);
+    }
+    const u32 n0 = pj & 255u, n1 = (pj >> 8) & 255u;   // at most SPARSE_N each
+    const u32 a0 = (n0 >= 32 ? ~0u : (1u << n0) - 1) & ~warp_or32(kill0);
+    const u32 a1 = (n1 >= 32 ? ~0u : (1u << n1) - 1) & ~warp_or32(kill1);
+    if (a0 | a1) {                                  // the task path goes on from the second round
+      again |= 1u << j;
+      if (lane == 0) { hand[j * HAND_WORDS] = a0; hand[j * HAND_WORDS + 1] = a1; }
+    }
+  }
+  __syncwarp();
+  return again;
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
   extern __shared__ __align__(16) u32 tab[];
@@ -516,6 +583,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
   // the stride descriptors (at most SMD_MAX, the host keeps any further strides unmasked)
   MaskDesc *smd = reinterpret_cast<MaskDesc *>(tab + SHORT_LANES * tab_words);
   for (u32 k = threadIdx.x; k < P.nm_all; k += BLOCK) smd[k] = P.mdesc[k];
+  u32 *hand = reinterpret_cast<u32 *>(smd + P.nm_all) + warp * 32 * HAND_WORDS;   // this warp's hand-on
   const u32 nshort = P.hdr->nshort;
   for (u32 l0 = blockIdx.x * SHORT_LANES; l0 < P.L; l0 += gridDim.x * SHORT_LANES) {
     for (int q = 0; q < SHORT_LANES; ++q) {
@@ -563,7 +631,16 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
           pk |= (nq << (8 * q)) | (bq << (24 + q));
         }
       }
-      unsigned todo = __ballot_sync(FULL, (pk & ((1u << (8 * SHORT_LANES)) - 1)) != 0);
+      u32 nmax_w = 0;
+      #pragma unroll
+      for (int q = 0; q < SHORT_LANES; ++q) nmax_w = max(nmax_w, (pk >> (8 * q)) & 255u);
+      unsigned todo = __ballot_sync(FULL, nmax_w > SPARSE_N);
+      unsigned hand_mask = 0;                      // windows the sparse round handed on
+      if (SPARSE_N) {
+        const unsigned sp = __ballot_sync(FULL, nmax_w > 0 && nmax_w <= SPARSE_N);
+        if (sp) hand_mask = short_sparse_round(P, tab, tab_words, md0, x.w, pk, sp, hand, lane);
+        todo |= hand_mask;
+      }
       u32 q0n = todo ? load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1)) : 0u;
       while (todo) {
         const int j = __ffs(todo) - 1;
@@ -580,18 +657,19 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
           nmax = max(nmax, n[q]);
         }
         const WinRef R{wi, x.x, x.y, j};
+        const u32 *hj = (hand_mask >> j) & 1u ? hand + j * HAND_WORDS : nullptr;
         // chunks per lane; one chunk is by far the commonest case, so it is tested first.
         const u32 nc = (nmax + 31) >> 5;
         // instantiations for 1, 2 and 4 chunks (8 too when SEG_SMALL is 256) measured faster
         // than one per chunk count: the kernel's code stays small enough for the instruction
         // cache
-        if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
-        else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
+        if (nc == 1) short_segments<1>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0, hj);
+        else if (nc == 2) short_segments<2>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0, hj);
         else if constexpr (SEG_SMALL > 128) {
-          if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
-          else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
+          if (nc <= 4) short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0, hj);
+          else short_segments<8>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0, hj);
         } else if constexpr (SEG_SMALL > 64) {
-          short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0);
+          short_segments<4>(P, tab, tab_words, smd, l0, R, rho, n, b, K0row, q0_first, lane, md0, hj);
         }
       }
     }
@@ -851,7 +929,8 @@ constexpr int MARK_BLOCK = 128;
 #ifndef ES_SHORT_BLOCK
 #define ES_SHORT_BLOCK 512
 #endif
-constexpr int SHORT_BLOCK = ES_SHORT_BLOCK;   // 16 warps, 64 registers: two CTAs of two 37 KB lane tables fill an SM
+constexpr int SHORT_BLOCK = ES_SHORT_BLOCK;
+constexpr size_t SHORT_HAND_BYTES = (size_t)(SHORT_BLOCK / 32) * 32 * HAND_WORDS * sizeof(u32);   // 16 warps, 64 registers: two CTAs of two 37 KB lane tables fill an SM
 
 }  // namespace es
 
@@ -1073,7 +1152,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
 }
 
 static size_t short_smem(const es_engine *e) {
-  return (size_t)SHORT_LANES * e->Wpad * 8 + (size_t)e->nm_all * sizeof(MaskDesc);
+  return (size_t)SHORT_LANES * e->Wpad * 8 + (size_t)e->nm_all * sizeof(MaskDesc) + SHORT_HAND_BYTES;
 }
 
 static size_t mark_smem(const es_engine *e) {
@@ -1785,7 +1864,8 @@ static es_status build_tables(es_engine *e) {
     }
     CU(cudaStreamSynchronize(bs));
     CU(cudaFuncSetAttribute(k_mark_short<SHORT_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc))));
+                            (int)(SHORT_LANES * (MASK_BYTES_MAX + 16) + SMD_MAX * sizeof(MaskDesc) +
+                                  SHORT_HAND_BYTES)));
   }
   CU(cudaStreamSynchronize(e->slots[0].stream));
   // occupancy of the marking kernel, for the persistent grid

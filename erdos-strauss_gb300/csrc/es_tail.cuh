@@ -322,60 +322,66 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
   return f;
 }
 
+// One helping pass of a warp with nothing else to do: pick a posted cofactor, walk HELP_STEPS
+// steps per lane with constants no other walk uses (or run a round of curves, with ecm), and
+// post the first divisor found. Returns 2 when every prime of the run is finished, 0 when the
+// board was empty, 1 otherwise. All lanes call.
+__device__ inline int warp_help_once(const HardBoard &B, u32 lane, bool ecm) {
+  if (ld_volatile(B.done) >= B.total) return 2;
+  const u32 st = lane < HARD_SLOTS ? ld_volatile(&B.slot[lane].state) : 0u;
+  const unsigned posted = __ballot_sync(FULL, st == 2u);
+  if (!posted) return 0;
+  u64 ses = 0;
+  if (lane == 0) ses = atomicAdd(B.sessions, 1ull);
+  ses = __shfl_sync(FULL, ses, 0);
+  u32 pick = (u32)(ses % (u64)__popc(posted)), j = 0;
+  for (unsigned m = posted;; m &= m - 1) {
+    if (pick-- == 0) { j = (u32)(__ffs(m) - 1); break; }
+  }
+  HardSlot *hs = &B.slot[j];
+  const u64 n = ld_volatile(&hs->n);
+  __threadfence();
+  if (ld_volatile(&hs->state) != 2u || n <= 0xFFFFFFFFull || !(n & 1)) return 1;
+  const Mont M = mont_init(n);
+  auto poll = [&](u64) -> u64 {
+    u64 ext = 0;
+    if (lane == 0)
+      ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
+    return __shfl_sync(FULL, ext, 0);
+  };
+  // A round of curves polls its slot every few ladder bits and every few giant steps, so it
+  // stops as soon as the cofactor is split; its sigmas lie above every owner's (an owner's round
+  // r uses 6 + 32 r + lane, r < ECM_OWNER_ROUNDS) and are distinct per session. Rho walks take
+  // constants above every owner's (an owner walks c = 1 + lane + 32 j with j below 2^12),
+  // distinct per session (2^20 sessions apart before a restart adds 2^25); a posted cofactor has
+  // already outlasted its owner's first walks, so helpers start with a longer window.
+  u64 d = 0;
+  if (ecm && n < LazyArith::NMAX) {
+    u64 ext = 0;
+    d = warp_ecm<LazyArith>(M, ECM_SIGMA_HELP + 32 * (ses & 0xFFFFFull), lane, [&]() -> u64 { return poll(0); },
+                            ext);
+  } else {
+    const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
+    d = n < LazyArith::NMAX ? rho_walk<LazyArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0)
+                            : rho_walk<ExactArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
+  }
+  if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
+    atomicCAS(&hs->found, 0ull, (unsigned long long)d);
+  __syncwarp();
+  return 1;
+}
+
 // A warp with nothing left to do helps the posted cofactors until every prime of the run is
 // finished (or the board stays empty for HELP_IDLE_POLLS polls, or after HELP_MAX_ROUNDS
-// sessions): each session picks a posted slot, walks HELP_STEPS steps per lane with constants
-// no other walk uses, and posts the first divisor it finds. All lanes call.
+// sessions). All lanes call.
 __device__ inline void warp_help(const HardBoard &B, u32 lane) {
   for (u32 idle = 0, round = 0; idle < HELP_IDLE_POLLS && round < HELP_MAX_ROUNDS + HELP_IDLE_POLLS; ++round) {
-    if (ld_volatile(B.done) >= B.total) return;
-    const u32 st = lane < HARD_SLOTS ? ld_volatile(&B.slot[lane].state) : 0u;
-    const unsigned posted = __ballot_sync(FULL, st == 2u);
-    if (!posted) {
+    const int h = warp_help_once(B, lane, ES_HELP_ECM);
+    if (h == 2) return;
+    if (h == 0) {
       ++idle;
       __nanosleep(ES_HELP_SLEEP_NS);
-      continue;
     }
-    u64 ses = 0;
-    if (lane == 0) ses = atomicAdd(B.sessions, 1ull);
-    ses = __shfl_sync(FULL, ses, 0);
-    u32 pick = (u32)(ses % (u64)__popc(posted)), j = 0;
-    for (unsigned m = posted;; m &= m - 1) {
-      if (pick-- == 0) { j = (u32)(__ffs(m) - 1); break; }
-    }
-    HardSlot *hs = &B.slot[j];
-    const u64 n = ld_volatile(&hs->n);
-    __threadfence();
-    if (ld_volatile(&hs->state) != 2u || n <= 0xFFFFFFFFull || !(n & 1)) continue;
-    const Mont M = mont_init(n);
-    auto poll = [&](u64) -> u64 {
-      u64 ext = 0;
-      if (lane == 0)
-        ext = (ld_volatile(&hs->state) != 2u || ld_volatile(&hs->n) != n || ld_volatile(&hs->found) != 0) ? ~0ull : 0;
-      return __shfl_sync(FULL, ext, 0);
-    };
-    // With ES_HELP_ECM a helper runs a round of curves, which polls its slot every few ladder
-    // bits and every few giant steps, so it stops as soon as the cofactor is split (rounds that
-    // could not stop early measured worse than rho walks). Otherwise it walks rho: constants
-    // above every owner's (an owner walks c = 1 + lane + 32 j with j below 2^12), distinct per
-    // session (2^20 sessions apart before a restart adds 2^25); a posted cofactor has already
-    // outlasted its owner's first walks, so helpers start with a longer window.
-    u64 d = 0;
-    if (ES_HELP_ECM && n < LazyArith::NMAX) {
-      // A round of 32 curves with sigmas above every owner's (an owner's round r uses
-      // 6 + 32 r + lane, r < ECM_OWNER_ROUNDS), distinct per session; it polls the slot every
-      // few ladder bits, so a helper leaves as soon as anyone has split the cofactor.
-      u64 ext = 0;
-      d = warp_ecm<LazyArith>(M, ECM_SIGMA_HELP + 32 * (ses & 0xFFFFFull), lane, [&]() -> u64 { return poll(0); },
-                              ext);
-    } else {
-      const u64 c0 = (1ull << 24) + 32 * (ses & 0xFFFFFull) + 1 + lane;
-      d = n < LazyArith::NMAX ? rho_walk<LazyArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0)
-                              : rho_walk<ExactArith>(n, M, c0, 1ull << 25, HELP_STEPS, lane, poll, ES_HELP_R0);
-    }
-    if (lane == 0 && d > 1 && d < n && n % d == 0 && ld_volatile(&hs->n) == n)
-      atomicCAS(&hs->found, 0ull, (unsigned long long)d);
-    __syncwarp();
   }
 }
 
@@ -609,6 +615,23 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
 
 struct RungResult { u64 A; u32 r, k; U128 u; };
 
+// Rung k of p's walk (the loop body of solve_rung3, sieve/rung_scan3.cpp:578-603): r = r0 + 4k
+// with r0 the least positive r = -p (mod 4), A = (p + r) / 4, q = pA, and the residue the
+// divisor must have, target = -q (mod r). False when the rung does not apply (r > RCAP, A = 0,
+// or q not prime to r).
+struct Rung { u64 A; U128 q; u32 r, target; };
+__device__ __forceinline__ u32 rung_r0(u64 p) { return 4 - (u32)(p & 3); }
+__device__ __forceinline__ bool rung_of(u64 p, u32 k, Rung &g) {
+  const u32 r = rung_r0(p) + 4 * k;
+  if (k > RCAP || r > RCAP) return false;
+  const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
+  if (!A) return false;
+  const u32 qm = (u32)(((p % r) * (A % r)) % r);
+  if (r > 1 && gcd64(qm, r) != 1) return false;
+  g = Rung{A, U128{p * A, __umul64hi(p, A)}, r, qm ? r - qm : 0};
+  return true;
+}
+
 // Below this bound a divisor of q^2 = (pA)^2 cannot involve p or a prime factor of a cofactor
 // that trial division left (every such prime is at least 65537, the first prime after the
 // trial-division table's last, 65521).
@@ -653,26 +676,20 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u3
                                        const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
                                        bool use_ecm = true) {
   const u32 lane = threadIdx.x & 31;
-  const u32 pm4 = (u32)(p & 3);
-  const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
-  for (u32 k = 0;; ++k) {
-    const u32 r = r0 + 4 * k;
-    if (r > RCAP) return false;
-    const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
-    if (!A) continue;
-    const u32 qm = (u32)(((p % r) * (A % r)) % r);
-    if (r > 1 && gcd64(qm, r) != 1) continue;
-    const u32 target = qm ? r - qm : 0;
-    const U128 q{p * A, __umul64hi(p, A)};
+  const u32 r0 = rung_r0(p);
+  for (u32 k = 0; r0 + 4 * k <= RCAP; ++k) {
+    Rung g;
+    if (!rung_of(p, k, g)) continue;
     U128 u;
-    if (!rung_divisor(p, A, q, r, target, F, D, tdp, tdi, status, lane, rho_slot, nullptr, 0, board, rho_budget,
-                      use_ecm, u))
+    if (!rung_divisor(p, g.A, g.q, g.r, g.target, F, D, tdp, tdi, status, lane, rho_slot, nullptr, 0, board,
+                      rho_budget, use_ecm, u))
       return false;
     if (u.lo == 0 && u.hi == 0) continue;
-    if (lane == 0) *out = RungResult{A, r, k, u};
+    if (lane == 0) *out = RungResult{g.A, g.r, k, u};
     __syncwarp();
     return true;
   }
+  return false;
 }
 
 // The rung walk of one prime by a block of W warps (solve_rung3, sieve/rung_scan3.cpp:
@@ -691,26 +708,19 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u
   }
   if (lane == 0) slot[w].k = 0x7FFFFFFF;
   __syncthreads();
-  const u32 pm4 = (u32)(p & 3);
-  const u32 r0 = (4 - pm4) % 4 ? (4 - pm4) % 4 : 4;
-  for (u32 k = w;; k += W) {
-    const u32 r = r0 + 4 * k;
-    if (r > RCAP) break;
+  const u32 r0 = rung_r0(p);
+  for (u32 k = w; r0 + 4 * k <= RCAP; k += W) {
     // warp-uniform: every lane must take the same branch before the warp collectives below
     if ((int)k >= __shfl_sync(FULL, *(volatile int *)best_k, 0)) break;
-    const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
-    if (!A) continue;
-    const u32 qm = (u32)(((p % r) * (A % r)) % r);
-    if (r > 1 && gcd64(qm, r) != 1) continue;
-    const u32 target = qm ? r - qm : 0;
-    const U128 q{p * A, __umul64hi(p, A)};
+    Rung g;
+    if (!rung_of(p, k, g)) continue;
     U128 u;
-    if (!rung_divisor(p, A, q, r, target, F[w], D[w], tdp, tdi, status, lane, rho_slot + w, best_k, (int)k, board,
-                      rho_budget, true, u))
+    if (!rung_divisor(p, g.A, g.q, g.r, g.target, F[w], D[w], tdp, tdi, status, lane, rho_slot + w, best_k, (int)k,
+                      board, rho_budget, true, u))
       break;
     if (u.lo == 0 && u.hi == 0) continue;
     if (lane == 0) {
-      slot[w] = RungResult{A, r, k, u};
+      slot[w] = RungResult{g.A, g.r, k, u};
       atomicMin(best_k, (int)k);
     }
     break;
