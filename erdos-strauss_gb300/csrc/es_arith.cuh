@@ -20,6 +20,7 @@ namespace es {
 
 typedef unsigned long long u64;
 typedef unsigned int u32;
+typedef unsigned short u16;
 
 // Device status bits (written with atomicOr, read by the host after each run).
 enum : u32 {

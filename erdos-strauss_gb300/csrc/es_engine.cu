@@ -786,6 +786,7 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   const u64 n = min((u64)*T.prime_count, T.cap);
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   __shared__ BlockHelp bhelp;
+  __shared__ TdSieve tds;
   HardBoard B;
   B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
   B.local = nullptr;                                 // the warp phase: no block-mates on one prime
@@ -813,7 +814,8 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
     const u32 si = T.primes[i];
     const Surv s = T.surv[si];
     const bool ok = !no_rung &&
-                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tdi, T.status, F, D, rho_slot, &best_k, slot, &res, &B,
+                    block_solve_rung<RUNG_WARPS>(s.p, T.tdp, T.tdi, T.tdqm, &tds, T.status, F, D, rho_slot, &best_k, slot,
+                                                 &res, &B,
                                                  T.rho_budget);
     if (threadIdx.x == 0) rung_result(T, s, si, ok, res);
     __syncthreads();
@@ -867,7 +869,9 @@ __global__ void k_probe_prime(const u64 *n, u64 count, unsigned char *out) {
 }
 __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_probe_rung(const u64 *p, u64 count, RecDev *out,
                                                                unsigned char *found, const u32 *tdp,
-                                                               const u64 *tdi, u32 *status, u64 rho_budget) {
+                                                               const u64 *tdi, const uint2 *tdqm, u32 *status,
+                                                               u64 rho_budget) {
+  __shared__ TdSieve tds;
   __shared__ WarpFac F[RUNG_WARPS];
   __shared__ DPWarp D[RUNG_WARPS];
   __shared__ u64 rho_slot[RUNG_WARPS];
@@ -875,8 +879,8 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_probe_r
   __shared__ RungResult slot[RUNG_WARPS];
   __shared__ RungResult res;
   for (u64 i = blockIdx.x; i < count; i += gridDim.x) {
-    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tdi, status, F, D, rho_slot, &best_k, slot, &res, nullptr,
-                                           rho_budget);
+    bool ok = block_solve_rung<RUNG_WARPS>(p[i], tdp, tdi, tdqm, &tds, status, F, D, rho_slot, &best_k, slot, &res,
+                                           nullptr, rho_budget);
     if (threadIdx.x == 0) {
       if (ok && !check_rung_cert(p[i], res.A, res.r, res.u)) { atomicOr(status, ST_CERT_BAD); ok = false; }
       found[i] = ok;
@@ -1033,6 +1037,7 @@ struct es_engine {
   uint32_t Wpad = 0, nm_cov = 0, nm_all = 0, nl_cov = 0, nl_all = 0, m_inter = 0;
   es::TdEntry *d_tde = nullptr;
   es::u64 *d_tdi = nullptr;
+  uint2 *d_tdqm = nullptr;              // {d, floor(2^32 / d)} for the same primes
   // slot 0: es_run_window / es_run_batch / probes; slots 1..SERVE_SLOTS: serving workers
   es::Slot slots[1 + es::SERVE_SLOTS];
   std::string last_error;
@@ -1146,7 +1151,7 @@ static TailParams tail_params(const es_engine *e, const Slot *sl) {
   T.board = reinterpret_cast<HardSlot *>(sl->d_ctr + 16);
   T.help_blocks = (u32)(e->sm_count * ES_HELP_BLOCKS_PER_SM / ES_HELP_BLOCKS_DIV);
   T.rho_budget = e->rho_budget;
-  T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.tdi = e->d_tdi; T.status = sl->d_status;
+  T.cnt = sl->d_cnt; T.tdp = e->d_tdp; T.tde = e->d_tde; T.tdi = e->d_tdi; T.tdqm = e->d_tdqm; T.status = sl->d_status;
   T.cap = sl->cap;
   return T;
 }
@@ -1742,6 +1747,7 @@ static es_status build_tables(es_engine *e) {
   CU(cudaMalloc(&e->d_tdp, tdp.size() * sizeof(u32)));
   CU(cudaMalloc(&e->d_tde, tde.size() * sizeof(TdEntry)));
   CU(cudaMalloc(&e->d_tdi, tde.size() * sizeof(u64)));
+  CU(cudaMalloc(&e->d_tdqm, tdp.size() * sizeof(uint2)));
   CU(cudaMalloc(&d_mods, std::max<size_t>(nf, 1) * sizeof(u64)));
   temps.p[0] = d_mods;
   CU(cudaMalloc(&d_ress, std::max<size_t>(nf, 1) * sizeof(u64)));
@@ -1762,6 +1768,9 @@ static es_status build_tables(es_engine *e) {
   std::vector<u64> tdi(tde.size());
   for (size_t i = 0; i < tde.size(); ++i) tdi[i] = tde[i].inv;
   CU(cudaMemcpyAsync(e->d_tdi, tdi.data(), tdi.size() * sizeof(u64), cudaMemcpyHostToDevice, bs));
+  std::vector<uint2> tdqm(tdp.size());
+  for (size_t i = 0; i < tdp.size(); ++i) tdqm[i] = make_uint2(tdp[i], (u32)((1ull << 32) / tdp[i]));
+  CU(cudaMemcpyAsync(e->d_tdqm, tdqm.data(), tdqm.size() * sizeof(uint2), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_mods, om.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_ress, orr.data(), nf * sizeof(u64), cudaMemcpyHostToDevice, bs));
   CU(cudaMemcpyAsync(d_g, og.data(), nf * sizeof(u32), cudaMemcpyHostToDevice, bs));
@@ -2165,7 +2174,7 @@ es_status es_close(es_engine *e) {
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   cudaFree(e->d_rho); cudaFree(e->d_fdesc); cudaFree(e->d_sdist); cudaFree(e->d_tdp);
-  cudaFree(e->d_K0); cudaFree(e->d_tde); cudaFree(e->d_tdi);
+  cudaFree(e->d_K0); cudaFree(e->d_tde); cudaFree(e->d_tdi); cudaFree(e->d_tdqm);
   cudaFree(e->d_mtab); cudaFree(e->d_mdesc); cudaFree(e->d_lfil);
   delete e;
   return ES_OK;
@@ -2390,7 +2399,7 @@ es_status es_solve_rung_batch(es_engine *e, const uint64_t *p, size_t count, es_
   return probe(e, &e->slots[0], count, count * 8, p, 0, {{out, count * sizeof(es_record)}, {found, count}},
                [&](void *in, std::vector<void *> &o) {
                  k_probe_rung<<<e->sm_count * 4, RUNG_WARPS * 32, 0, e->slots[0].stream>>>((const u64 *)in, count, (RecDev *)o[0],
-                                                                     (unsigned char *)o[1], e->d_tdp, e->d_tdi,
+                                                                     (unsigned char *)o[1], e->d_tdp, e->d_tdi, e->d_tdqm,
                                                                      e->slots[0].d_status, e->rho_budget);
                });
 }

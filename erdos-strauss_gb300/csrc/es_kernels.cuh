@@ -5,8 +5,6 @@
 
 namespace es {
 
-typedef unsigned short u16;
-
 constexpr u16 K0_MISS = 0xFFFF;     // the filter never hits this lane
 constexpr int DMAX = 8192;          // distinct strides held in shared memory per CTA
 
@@ -142,6 +140,7 @@ struct TailParams {
   const u32 *tdp;          // odd primes < 2^16
   const TdEntry *tde;      // their inverses mod 2^64 and division limits (thread-per-value paths)
   const u64 *tdi;          // their inverses mod 2^64 alone (warp trial division)
+  const uint2 *tdqm;       // {d, floor(2^32 / d)} (the rung sieve's residues)
   u32 *status;
   u64 cap;                 // capacity of surv/primes/direct/recs
   unsigned long long *rung_next;      // k_rung's prime queue head, whole blocks (the tail)

@@ -452,6 +452,80 @@ __device__ inline bool warp_factor_cofactor(u64 v0, WarpFac &F, u32 *status, u32
   return true;
 }
 
+// The odd primes below 2^16 dividing each rung of one prime, found for all rungs at once:
+// rung k's A is A_k = floor(p/4) + 1 + k (A = (p + r)/4 with r = r0 + 4k and p + r0 = 4
+// floor(p/4) + 4), so q | A_k exactly when k = -A_0 (mod q), and one residue A_0 mod q per
+// prime q replaces trial division of every rung by q. The 17 primes below TD_RUNGS divide many
+// rungs each and are kept as a bit mask per rung; every larger prime divides at most one of
+// the 64 rungs and goes into that rung's list. Rung k then divides out only its own primes; a
+// list longer than TD_LIST_CAP is marked incomplete and that rung trial-divides.
+constexpr int TD_RUNGS = 64;            // rung indices 0 .. 63 (r = r0 + 4k <= RCAP)
+constexpr int TD_SMALL = 17;            // odd primes below TD_RUNGS: 3 .. 61, tdp[0 .. 16]
+constexpr int TD_LIST_CAP = 15;         // with TD_SMALL, at most 32: one prime per lane
+struct TdSieve {                        // shared memory, one per block
+  u16 idx[TD_RUNGS][TD_LIST_CAP];       // indices into tdp of the primes above 61 dividing A_k
+  u32 n[TD_RUNGS];                      // their count (above TD_LIST_CAP: the list is incomplete)
+  u32 small[TD_RUNGS];                  // bit i: tdp[i] divides A_k, i < TD_SMALL
+  uint2 qm[TD_SMALL];                   // tdp[i] and floor(2^32 / tdp[i])
+  u32 rs[TD_SMALL];                     // A_0 mod tdp[i]
+};
+
+// x mod q for x < 2^32 and an odd prime q < 2^16, m = floor(2^32 / q) (Barrett: the
+// quotient estimate umulhi(x, m) is low by at most one).
+__device__ __forceinline__ u32 mod_q16(u32 x, u32 q, u32 m) {
+  const u32 r = x - __umulhi(x, m) * q;
+  return r >= q ? r - q : r;
+}
+__device__ __forceinline__ u32 mod_a0(u32 hi, u32 mid, u32 lo, u32 q, u32 m) {   // A0 mod q, 16 bits at a time
+  u32 r = mod_q16(hi, q, m);
+  r = mod_q16((r << 16) | mid, q, m);
+  return mod_q16((r << 16) | lo, q, m);
+}
+
+// S for A_k = A0 + k, k < TD_RUNGS, A0 < 2^64, from tdqm[i] = {d_i, floor(2^32 / d_i)} over
+// the odd primes d_i below 2^16. Each thread takes SIEVE_BATCH primes at a time, their table
+// entries loaded together before any is used. Every thread of the block calls; the block
+// synchronizes on entry and exit.
+constexpr int SIEVE_BATCH = 8;
+__device__ inline void block_td_sieve(u64 A0, const uint2 *__restrict__ tdqm, TdSieve &S) {
+  const u32 hi = (u32)(A0 >> 32), mid = (u32)(A0 >> 16) & 0xFFFFu, lo = (u32)A0 & 0xFFFFu;
+  for (int k = threadIdx.x; k < TD_RUNGS; k += blockDim.x) S.n[k] = 0;
+  if (threadIdx.x < TD_SMALL) {
+    const uint2 e = __ldg(tdqm + threadIdx.x);
+    S.qm[threadIdx.x] = e;
+    S.rs[threadIdx.x] = mod_a0(hi, mid, lo, e.x, e.y);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < TD_RUNGS; k += blockDim.x) {   // the small primes, rung by rung
+    u32 mask = 0;
+    #pragma unroll
+    for (int i = 0; i < TD_SMALL; ++i) {
+      const uint2 e = S.qm[i];
+      if (mod_q16(S.rs[i] + (u32)k, e.x, e.y) == 0) mask |= 1u << i;
+    }
+    S.small[k] = mask;
+  }
+  for (int i0 = TD_SMALL + threadIdx.x; i0 < NTD; i0 += SIEVE_BATCH * blockDim.x) {
+    uint2 e[SIEVE_BATCH];
+    #pragma unroll
+    for (int j = 0; j < SIEVE_BATCH; ++j) {
+      const int i = i0 + j * (int)blockDim.x;
+      e[j] = i < NTD ? __ldg(tdqm + i) : make_uint2(0u, 0u);
+    }
+    #pragma unroll
+    for (int j = 0; j < SIEVE_BATCH; ++j) {
+      if (!e[j].x) continue;
+      const u32 r = mod_a0(hi, mid, lo, e[j].x, e[j].y);
+      const u32 k = r ? e[j].x - r : 0u;                 // q > TD_RUNGS: one rung at most
+      if (k < (u32)TD_RUNGS) {
+        const u32 s = atomicAdd(&S.n[k], 1u);
+        if (s < (u32)TD_LIST_CAP) S.idx[k][s] = (u16)(i0 + j * (int)blockDim.x);
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // Complete factorization of n >= 1 into F (prime order as found). All lanes call.
 // Returns false when a bound was hit (status says which). With hard_left, a composite
 // cofactor that would need rho (no prime factor below 2^16, not a square) is not factored:
@@ -461,7 +535,8 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
                                    u32 *status, u32 lane, volatile u64 *rho_slot,
                                    const volatile int *cancel = nullptr, int my_k = 0,
                                    const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS,
-                                   bool use_ecm = true, u64 *hard_left = nullptr) {
+                                   bool use_ecm = true, u64 *hard_left = nullptr,
+                                   const u16 *td_list = nullptr, u32 td_n = ~0u, u32 td_small = 0) {
   if (hard_left) *hard_left = 0;
   if (lane == 0) { F.k = 0; F.overflow = 0; }
   __syncwarp();
@@ -478,6 +553,59 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
   // than one per block. Testing primes past the point where d^2 > cur is harmless (each prime
   // is tested once, against n, and a hit is a genuine factor), so the early exit is checked
   // once per block.
+  // Divides out of cur every prime of this chunk that divides n (hit: x = n / d exactly), with
+  // its full power, and records it in F.
+  auto take = [&](bool hit, u64 x, u64 iv, u32 d) {
+    const unsigned mask = __ballot_sync(FULL, hit);
+    if (!mask) return;                             // rare: a prime below 2^16 divides n
+    u64 f = 1;
+    int e = 0;
+    if (hit) {
+      u64 m = x;
+      e = 1;
+      f = iv;
+      for (int g = 0; g < 64; ++g) {
+        x = m * iv;
+        if (__umul64hi(x, (u64)d)) break;
+        m = x; ++e; f *= iv;
+      }
+    }
+    const int base = F.k;
+    __syncwarp();
+    if (hit) {
+      const int pos = base + __popc(mask & ((1u << lane) - 1));
+      if (pos < MAXF) { F.pr[pos] = d; F.ex[pos] = e; }
+    }
+    u64 g = f;
+    #pragma unroll
+    for (int o = 16; o; o >>= 1) g *= __shfl_xor_sync(FULL, g, o);
+    cur *= g;                                      // exact: divides out every d^e found
+    __syncwarp();
+    if (lane == 0) {
+      const int nk = base + __popc(mask);
+      if (nk > MAXF) F.overflow = 1;
+      F.k = nk > MAXF ? MAXF : nk;
+    }
+    __syncwarp();
+  };
+  if (td_list && td_n <= (u32)TD_LIST_CAP) {       // the block's sieve listed n's odd primes < 2^16
+    const u32 ns = __popc(td_small);               // lanes [0, ns): the small ones, then the list
+    bool mine = false;
+    u32 i = 0;
+    if (lane < ns) {
+      u32 m = td_small;
+      for (u32 t = 0; t < lane; ++t) m &= m - 1;
+      i = (u32)(__ffs(m) - 1);
+      mine = true;
+    } else if (lane < ns + td_n) {
+      i = (u32)td_list[lane - ns];
+      mine = true;
+    }
+    const u64 iv = mine ? __ldg(tdi + i) : 0;
+    const u32 d = mine ? __ldg(tdp + i) : 0u;
+    const u64 x = n * iv;
+    take(mine && __umul64hi(x, (u64)d) == 0, x, iv, d);
+  } else {
   constexpr int TD_UNROLL = 8;
   u64 inv[TD_UNROLL], ninv[TD_UNROLL];
   u32 pr[TD_UNROLL], npr[TD_UNROLL];
@@ -496,40 +624,8 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
     #pragma unroll
     for (int j = 0; j < TD_UNROLL; ++j) {
       const int i = (cb + j) * 32 + lane;
-      u64 x = n * inv[j];
-      const bool hit = i < NTD && __umul64hi(x, (u64)pr[j]) == 0;
-      const unsigned mask = __ballot_sync(FULL, hit);
-      if (mask) {                                  // rare: a prime below 2^16 divides n
-        u64 f = 1;
-        int e = 0;
-        if (hit) {
-          u64 m = x;
-          e = 1;
-          f = inv[j];
-          for (int g = 0; g < 64; ++g) {
-            x = m * inv[j];
-            if (__umul64hi(x, (u64)pr[j])) break;
-            m = x; ++e; f *= inv[j];
-          }
-        }
-        const int base = F.k;
-        __syncwarp();
-        if (hit) {
-          const int pos = base + __popc(mask & ((1u << lane) - 1));
-          if (pos < MAXF) { F.pr[pos] = pr[j]; F.ex[pos] = e; }
-        }
-        u64 g = f;
-        #pragma unroll
-        for (int o = 16; o; o >>= 1) g *= __shfl_xor_sync(FULL, g, o);
-        cur *= g;                                  // exact: divides out every d^e found
-        __syncwarp();
-        if (lane == 0) {
-          const int nk = base + __popc(mask);
-          if (nk > MAXF) F.overflow = 1;
-          F.k = nk > MAXF ? MAXF : nk;
-        }
-        __syncwarp();
-      }
+      const u64 x = n * inv[j];
+      take(i < NTD && __umul64hi(x, (u64)pr[j]) == 0, x, inv[j], pr[j]);
     }
     if (nx >= NTD) break;
     const u64 dn = __shfl_sync(FULL, (u64)npr[0], 0);   // the next block's first prime
@@ -537,6 +633,7 @@ __device__ inline bool warp_factor(u64 n, WarpFac &F, const u32 *__restrict__ td
     if (cancel && __shfl_sync(FULL, cancelled(cancel, my_k) ? 1 : 0, 0)) return false;   // moot rung
     #pragma unroll
     for (int j = 0; j < TD_UNROLL; ++j) { inv[j] = ninv[j]; pr[j] = npr[j]; }
+  }
   }
   if (cur > 1) {
     if (!complete || cur <= 0xFFFFFFFFull) {
@@ -650,10 +747,11 @@ constexpr u64 SMALL_U_BOUND = 65536;
 __device__ inline bool rung_divisor(u64 p, u64 A, U128 q, u32 r, u32 target, WarpFac &F, DPWarp &D,
                                     const u32 *tdp, const u64 *tdi, u32 *status, u32 lane,
                                     volatile u64 *rho_slot, const volatile int *cancel, int my_k,
-                                    const HardBoard *board, u64 rho_budget, bool use_ecm, U128 &u) {
+                                    const HardBoard *board, u64 rho_budget, bool use_ecm, U128 &u,
+                                    const u16 *td_list = nullptr, u32 td_n = ~0u, u32 td_small = 0) {
   u64 hard = 0;
   if (!warp_factor(A, F, tdp, tdi, status, lane, rho_slot, cancel, my_k, board, rho_budget, use_ecm,
-                   ES_SMALL_U ? &hard : nullptr))
+                   ES_SMALL_U ? &hard : nullptr, td_list, td_n, td_small))
     return false;
   if (hard) {
     u = warp_min_div_res(p, F, U128{SMALL_U_BOUND, 0}, r, target, D, lane);
@@ -692,14 +790,20 @@ __device__ inline bool warp_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u3
   return false;
 }
 
+#ifndef ES_TD_SIEVE
+#define ES_TD_SIEVE 1
+#endif
 // The rung walk of one prime by a block of W warps (solve_rung3, sieve/rung_scan3.cpp:
 // 578-603). Warp w takes rung indices k = w, w+W, ... (r = r0 + 4k) in increasing order and
-// stops once k passes the best certifying index found by any warp. Returns true in every
-// thread when some rung certifies p; the block's result is then in *out.
+// stops once k passes the best certifying index found by any warp. With S the block first
+// lists the odd primes below 2^16 of all the prime's rungs at once (block_td_sieve), and each
+// rung divides out only its own. Returns true in every thread when some rung certifies p;
+// the block's result is then in *out.
 template <int W>
-__device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u32 *status, WarpFac *F, DPWarp *D,
-                                 volatile u64 *rho_slot, int *best_k, RungResult *slot, RungResult *out,
-                                 const HardBoard *board = nullptr, u64 rho_budget = WARP_RHO_STEPS) {
+__device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, const uint2 *tdqm, TdSieve *S,
+                                        u32 *status, WarpFac *F, DPWarp *D, volatile u64 *rho_slot, int *best_k,
+                                        RungResult *slot, RungResult *out, const HardBoard *board = nullptr,
+                                        u64 rho_budget = WARP_RHO_STEPS) {
   const u32 lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   BlockHelp *const bh = board ? board->local : nullptr;
   if (threadIdx.x == 0) {
@@ -708,6 +812,8 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u
   }
   if (lane == 0) slot[w].k = 0x7FFFFFFF;
   __syncthreads();
+  if (!ES_TD_SIEVE) S = nullptr;
+  if (S) block_td_sieve((p >> 2) + 1, tdqm, *S);   // A_0 = floor(p/4) + 1
   const u32 r0 = rung_r0(p);
   for (u32 k = w; r0 + 4 * k <= RCAP; k += W) {
     // warp-uniform: every lane must take the same branch before the warp collectives below
@@ -716,7 +822,7 @@ __device__ inline bool block_solve_rung(u64 p, const u32 *tdp, const u64 *tdi, u
     if (!rung_of(p, k, g)) continue;
     U128 u;
     if (!rung_divisor(p, g.A, g.q, g.r, g.target, F[w], D[w], tdp, tdi, status, lane, rho_slot + w, best_k, (int)k,
-                      board, rho_budget, true, u))
+                      board, rho_budget, true, u, S ? S->idx[k] : nullptr, S ? S->n[k] : ~0u, S ? S->small[k] : 0u))
       break;
     if (u.lo == 0 && u.hi == 0) continue;
     if (lane == 0) {
