@@ -53,9 +53,9 @@ MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
     (128, 1): {"inst": 784637251, "dram": 94985984 + 3377920},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
-    4: {"inst": 79067229, "dram": 814592},
-    6: {"inst": 79324859, "dram": 808448},
-    8: {"inst": 79292614, "dram": 817152},
+    4: {"inst": 79429266, "dram": 853248},
+    6: {"inst": 79412528, "dram": 852736},
+    8: {"inst": 79795257, "dram": 850176},
 }
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
