@@ -746,7 +746,10 @@ constexpr int RUNG_WARPS = ES_RUNG_WARPS;
 #define ES_RUNG_MIN_BLOCKS (16 / RUNG_WARPS)   // resident blocks per SM the register budget allows
 #endif
 #ifndef ES_HELP_BLOCKS_PER_SM
-#define ES_HELP_BLOCKS_PER_SM 0
+#define ES_HELP_BLOCKS_PER_SM 1
+#endif
+#ifndef ES_HELP_FEW_DIV
+#define ES_HELP_FEW_DIV 16
 #endif
 #ifndef ES_HELP_BLOCKS_DIV
 #define ES_HELP_BLOCKS_DIV 1
@@ -824,8 +827,15 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   // cofactor progress at the issue rate their sub-partition gives them, so helpers beyond
   // one warp per scheduler would only split that rate over more walks, and the expected wait
   // for the first collision grows with the square root of the number of walks sharing it.
+  // They help only a run of few primes (at most one per ES_HELP_FEW_DIV blocks), whose time
+  // is its slowest factorization on SMs that are otherwise idle: the 2^34 window at 1.8e19
+  // with the tuned table (21 primes) 0.33 against 0.46 ms of stage D. With more primes the
+  // helpers' walks take issue slots from the owners (129 primes: 0.375 against 0.36 ms;
+  // batches: 0.48 against 0.435 ms before this rule), and a pipelined tail would keep its
+  // blocks resident.
   B.local = nullptr;
-  if (!no_rung && blockIdx.x < T.help_blocks) warp_help(B, lane);
+  const bool few = ES_HELP_FEW_DIV == 0 || n * ES_HELP_FEW_DIV <= (u64)gridDim.x;
+  if (!no_rung && few && blockIdx.x < T.help_blocks) warp_help(B, lane);
 }
 
 __global__ void k_direct(const TailParams T) {
