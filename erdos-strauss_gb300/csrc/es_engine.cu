@@ -537,6 +537,9 @@ __device__ __forceinline__ void short_segments(const ShortParams &P, const u32 *
 // words left in hand[window][lane], and the task path goes on with them from the second round.
 // Counters and survivors are the task path's alone.
 
+// SH is the first round's row layout, the same for every stride of the round: 5 when its rows
+// are interleaved (word w of the stride in slot j at 32 w + j), 0 when they are packed.
+template <u32 SH>
 __device__ __forceinline__ unsigned short_sparse_round(const ShortParams &P, const u32 *tab, u32 tab_words,
                                                        const MaskDesc &md0, u32 xwi, u32 pk, unsigned sp,
                                                        u32 *hand, u32 lane) {
@@ -555,12 +558,12 @@ __device__ __forceinline__ unsigned short_sparse_round(const ShortParams &P, con
     if (has) {
       u32 r = qd + ((pj >> 24) & 1u);
       r = r >= md0.s ? r - md0.s : r;
-      const u32 *wp = tab + md0.off + ((r >> 5) << md0.sh);
-      kill0 = __funnelshift_r(wp[0], wp[1u << md0.sh], r & 31);
+      const u32 *wp = tab + md0.off + ((r >> 5) << SH);
+      kill0 = __funnelshift_r(wp[0], wp[1u << SH], r & 31);
       r = qd + ((pj >> 25) & 1u);
       r = r >= md0.s ? r - md0.s : r;
-      wp = tab + tab_words + md0.off + ((r >> 5) << md0.sh);
-      kill1 = __funnelshift_r(wp[0], wp[1u << md0.sh], r & 31);
+      wp = tab + tab_words + md0.off + ((r >> 5) << SH);
+      kill1 = __funnelshift_r(wp[0], wp[1u << SH], r & 31);
     }
     const u32 n0 = pj & 255u, n1 = (pj >> 8) & 255u;   // at most SPARSE_N each
     const u32 a0 = (n0 >= 32 ? ~0u : (1u << n0) - 1) & ~warp_or32(kill0);
@@ -609,6 +612,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
     constexpr u32 WS = BLOCK / 32;
     const uint4 *sw4 = reinterpret_cast<const uint4 *>(P.shortw);
     const MaskDesc md0 = lane < P.nm_cov ? smd[lane] : MaskDesc{1, 0, 0, 0};   // the first round's stride
+    const u32 sh0 = P.nm_cov ? smd[0].sh : 0u;          // its layout (the same for the round's strides)
     const u32 d_first = md0.d;
     auto load_q0 = [&](u32 wi) {
       return lane < P.nm_cov ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + d_first) : 0u;
@@ -638,7 +642,8 @@ __global__ void __launch_bounds__(BLOCK, 2) k_mark_short(const ShortParams P) {
       unsigned hand_mask = 0;                      // windows the sparse round handed on
       if (SPARSE_N) {
         const unsigned sp = __ballot_sync(FULL, nmax_w > 0 && nmax_w <= SPARSE_N);
-        if (sp) hand_mask = short_sparse_round(P, tab, tab_words, md0, x.w, pk, sp, hand, lane);
+        if (sp) hand_mask = sh0 ? short_sparse_round<5>(P, tab, tab_words, md0, x.w, pk, sp, hand, lane)
+                                : short_sparse_round<0>(P, tab, tab_words, md0, x.w, pk, sp, hand, lane);
         todo |= hand_mask;
       }
       u32 q0n = todo ? load_q0(__shfl_sync(FULL, x.w, __ffs(todo) - 1)) : 0u;
