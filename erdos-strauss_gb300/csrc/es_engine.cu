@@ -547,11 +547,16 @@ __device__ __forceinline__ unsigned short_sparse_round(const ShortParams &P, con
   const bool has = lane < P.nm_cov;                // lane k holds the first round's stride k
   auto ldq = [&](u32 wi) { return has ? (u32)__ldg(P.Qm + (size_t)wi * P.Dq + md0.d) : 0u; };
   unsigned again = 0;
+  // this lane's own window of the group: its positions in the CTA's two lanes as bit masks
+  // (at most SPARSE_N each when the window is sparse)
+  const u32 n0l = pk & 255u, n1l = (pk >> 8) & 255u;
+  const u32 lm0 = n0l >= 32 ? ~0u : (1u << n0l) - 1, lm1 = n1l >= 32 ? ~0u : (1u << n1l) - 1;
   u32 qn = ldq(__shfl_sync(FULL, xwi, __ffs(sp) - 1));
   while (sp) {
     const int j = __ffs(sp) - 1;
     sp &= sp - 1;
     const u32 pj = __shfl_sync(FULL, pk, j);
+    const u32 m0 = __shfl_sync(FULL, lm0, j), m1 = __shfl_sync(FULL, lm1, j);
     const u32 qd = qn;
     if (sp) qn = ldq(__shfl_sync(FULL, xwi, __ffs(sp) - 1));
     u32 kill0 = 0, kill1 = 0;
@@ -560,14 +565,15 @@ __device__ __forceinline__ unsigned short_sparse_round(const ShortParams &P, con
       r = r >= md0.s ? r - md0.s : r;
       const u32 *wp = tab + md0.off + ((r >> 5) << SH);
       kill0 = __funnelshift_r(wp[0], wp[1u << SH], r & 31);
-      r = qd + ((pj >> 25) & 1u);
-      r = r >= md0.s ? r - md0.s : r;
+      if ((pj ^ (pj >> 1)) & (1u << 24)) {       // the two lanes' segments start apart (rare)
+        r = qd + ((pj >> 25) & 1u);
+        r = r >= md0.s ? r - md0.s : r;
+      }
       wp = tab + tab_words + md0.off + ((r >> 5) << SH);
       kill1 = __funnelshift_r(wp[0], wp[1u << SH], r & 31);
     }
-    const u32 n0 = pj & 255u, n1 = (pj >> 8) & 255u;   // at most SPARSE_N each
-    const u32 a0 = (n0 >= 32 ? ~0u : (1u << n0) - 1) & ~warp_or32(kill0);
-    const u32 a1 = (n1 >= 32 ? ~0u : (1u << n1) - 1) & ~warp_or32(kill1);
+    const u32 a0 = m0 & ~warp_or32(kill0);
+    const u32 a1 = m1 & ~warp_or32(kill1);
     if (a0 | a1) {                                  // the task path goes on from the second round
       again |= 1u << j;
       if (lane == 0) { hand[j * HAND_WORDS] = a0; hand[j * HAND_WORDS + 1] = a1; }
