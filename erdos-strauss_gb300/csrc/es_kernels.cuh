@@ -49,9 +49,10 @@ struct Surv {
 };
 
 // Per-window device counters; covered/sieved/mr are derived on the host from
-// positions, alive-after-covers and survivors, which are sums over segments.
+// positions, alive-after-covers and survivors, which are sums over segments, and the
+// composites from the survivors less the primes (rung + direct + unsolved).
 struct WinCount {
-  unsigned long long positions, after_covers, surv, composite, rung, direct, unsolved, pad;
+  unsigned long long positions, after_covers, surv, spare, rung, direct, unsolved, pad;
 };
 
 // Device record: the layout of es_record.
