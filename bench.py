@@ -48,9 +48,9 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # k_mark_short's depend on (short_max, long_split), k_rung's on rung_blocks_per_sm. A schedule
 # with no capture here gets no issue figure rather than another schedule's.
 MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
-    (32, 1): {"inst": 826632339, "dram": 95779584 + 3481344},
-    (64, 1): {"inst": 768759852, "dram": 95262720 + 3449344},
-    (128, 1): {"inst": 784637251, "dram": 94985984 + 3377920},
+    (32, 1): {"inst": 734442333, "dram": 95898880 + 3676672},
+    (64, 1): {"inst": 724482591, "dram": 95406336 + 3820288},
+    (128, 1): {"inst": 745716421, "dram": 95081216 + 3645440},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
     4: {"inst": 79429266, "dram": 853248},
