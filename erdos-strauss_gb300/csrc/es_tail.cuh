@@ -667,20 +667,41 @@ struct DPWarp {            // shared memory, one per warp
   U128 nxt[RCAP + 1];
 };
 
+// Residues modulo a rung's r (1 <= r <= RCAP) without a division per residue: Barrett
+// reduction of 32-bit values with m = floor((2^32 - 1) / r) (the quotient estimate umulhi(x, m)
+// is low by at most one, r = 1 and powers of two included), and 64-bit values from their
+// halves with c = 2^32 mod r.
+struct ModR {
+  u32 r, m, c;
+  __device__ __forceinline__ explicit ModR(u32 r_) : r(r_), m(0xFFFFFFFFu / r_) {
+    const u32 rem = 0xFFFFFFFFu - m * r_;
+    c = rem + 1 == r_ ? 0u : rem + 1;
+  }
+  __device__ __forceinline__ u32 mod32(u32 x) const {
+    const u32 v = x - __umulhi(x, m) * r;
+    return v >= r ? v - r : v;
+  }
+  __device__ __forceinline__ u32 mod64(u64 x) const {
+    return mod32(mod32((u32)(x >> 32)) * c + mod32((u32)x));   // below RCAP^2 + RCAP < 2^32
+  }
+};
+
 // min_div_res (sieve/rung_scan3.cpp:544-565), lanes over residue classes. Returns the
 // least divisor u <= q of q^2 with u == target (mod r), or 0.
 __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, u32 target, DPWarp &D, u32 lane) {
   const U128 INF{~0ull, ~0ull};
-  for (u32 t = lane; t < r; t += 32) D.cur[t] = (t == 1 % r) ? U128{1, 0} : INF;
+  const ModR R(r);
+  const u32 one = r == 1 ? 0u : 1u;              // 1 mod r
+  for (u32 t = lane; t < r; t += 32) D.cur[t] = (t == one) ? U128{1, 0} : INF;
   __syncwarp();
   for (int idx = -1; idx < F.k; ++idx) {
     const u64 pr = idx < 0 ? p : F.pr[idx];
     const int e = idx < 0 ? 2 : 2 * (int)F.ex[idx];
-    const u32 prm = (u32)(pr % r);
+    const u32 prm = R.mod64(pr);
     u32 inv = 0;                                 // prm^-1 mod r (prm is a unit: gcd(q, r) = 1)
     for (u32 base = 0; base < r; base += 32) {
       const u32 x = base + lane;
-      const unsigned m = __ballot_sync(FULL, x < r && (prm * x) % r == 1 % r);
+      const unsigned m = __ballot_sync(FULL, x < r && R.mod32(prm * x) == one);
       if (m) { inv = base + __ffs(m) - 1; break; }
     }
     for (u32 t = lane; t < r; t += 32) {
@@ -692,7 +713,7 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
           bool over;
           pw = mul128_64(pw, pr, over);
           if (over || lt128(q, pw)) break;       // pr^j > q: nothing further fits
-          s = (s * inv) % r;
+          s = R.mod32(s * inv);
         }
         const U128 v = D.cur[s];
         if (v.lo == ~0ull && v.hi == ~0ull) continue;
@@ -723,7 +744,8 @@ __device__ __forceinline__ bool rung_of(u64 p, u32 k, Rung &g) {
   if (k > RCAP || r > RCAP) return false;
   const u64 A = (p >> 2) + ((u64)(p & 3) + r) / 4;
   if (!A) return false;
-  const u32 qm = (u32)(((p % r) * (A % r)) % r);
+  const ModR R(r);
+  const u32 qm = R.mod32(R.mod64(p) * R.mod64(A));
   if (r > 1 && gcd64(qm, r) != 1) return false;
   g = Rung{A, U128{p * A, __umul64hi(p, A)}, r, qm ? r - qm : 0};
   return true;
