@@ -169,6 +169,41 @@ __device__ __forceinline__ bool sprp_ar(u64 bm, u64 d, int s, const Mont &M) {
   return false;
 }
 
+// The base-2 round by left-to-right square-and-double: 2^d with a squaring per bit of d and,
+// for each set bit, a multiplication by the base that is a modular doubling, so only the
+// squarings take Montgomery multiplies (about 63 instead of about 95 for right-to-left binary
+// exponentiation). The same x comes out: Ar::norm gives its exact representative.
+template <class Ar>
+__device__ __forceinline__ bool sprp2_ar(u64 d, int s, const Mont &M) {
+  const u64 mone = M.n - M.one;
+  u64 x = Ar::add(M.one, M.one, M);                  // 2: the top bit of d (d >= 1)
+  for (int i = 62 - __clzll((long long)d); i >= 0; --i) {
+    x = Ar::mul(x, x, M);
+    if ((d >> i) & 1) x = Ar::add(x, x, M);
+  }
+  x = Ar::norm(x, M);
+  if (x == M.one || x == mone) return true;
+  for (int i = 1; i < s; ++i) {
+    x = Ar::norm(Ar::mul(x, x, M), M);
+    if (x == mone) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ bool sprp2_mont(u64 d, int s, const Mont &M) {
+  const u64 mone = M.n - M.one;
+  u64 x = addmod(M.one, M.one, M.n);
+  for (int i = 62 - __clzll((long long)d); i >= 0; --i) {
+    x = mmul(x, x, M);
+    if ((d >> i) & 1) x = addmod(x, x, M.n);
+  }
+  if (x == M.one || x == mone) return true;
+  for (int i = 1; i < s; ++i) {
+    x = mmul(x, x, M);
+    if (x == mone) return true;
+  }
+  return false;
+}
+
 __constant__ const u64 MR_BASES[12] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
 
 // The reference's is_prime: trial division by the 12 bases, then all 12 SPRP rounds
@@ -203,8 +238,7 @@ __device__ inline bool sprp2_64(u64 n) {
   u64 d = n - 1;
   const int s = __ffsll((long long)d) - 1;
   d >>= s;
-  const u64 two = addmod(M.one, M.one, n);
-  return n < LazyArith::NMAX ? sprp_ar<LazyArith>(two, d, s, M) : sprp_mont(two, d, s, M);
+  return n < LazyArith::NMAX ? sprp2_ar<LazyArith>(d, s, M) : sprp2_mont(d, s, M);
 }
 
 // ---------------------------------------------------------------- gcd, isqrt

@@ -1,7 +1,8 @@
 // Host build of the device ECM (erdos-strauss_gb300/csrc/es_ecm.cuh) for the CPU tests: the
 // same source compiled by g++ with the four device intrinsics it uses defined on 128-bit host
-// integers. Checks the lazy Montgomery multiply against exact residues and the lazy
-// strong-probable-prime round against the exact one, then runs 32 curves (sigma 6..37, one
+// integers. Checks the lazy Montgomery multiply against exact residues, the lazy
+// strong-probable-prime round against the exact one and the base-2 round by square-and-double
+// against the binary one, then runs 32 curves (sigma 6..37, one
 // warp's first round) on seeded 62-bit semiprimes with prime factors of 18-31 bits in the lazy
 // arithmetic the engine uses and prints the fraction of curves that split each size; the exact
 // arithmetic must find the same divisors curve for curve, and every divisor returned must
@@ -17,6 +18,7 @@ static inline unsigned long long __umul64hi(unsigned long long a, unsigned long 
   return (unsigned long long)(((unsigned __int128)a * b) >> 64);
 }
 static inline int __ffsll(long long x) { return x ? __builtin_ctzll((unsigned long long)x) + 1 : 0; }
+static inline int __clzll(long long x) { return x ? __builtin_clzll((unsigned long long)x) : 64; }
 static inline unsigned atomicOr(unsigned *p, unsigned v) { const unsigned o = *p; *p |= v; return o; }
 #include "es_ecm.cuh"
 using namespace es;
@@ -72,6 +74,12 @@ int main(int argc, char **argv) {
         printf("FAIL lazy sprp n=%llu base=%llu\n", n, b);
         return 1;
       }
+    }
+    // the base-2 round by square-and-double, in both arithmetics, against the binary one
+    const bool two = sprp_mont(to_mont(2, M), d, sh, M);
+    if (sprp2_ar<LazyArith>(d, sh, M) != two || sprp2_mont(d, sh, M) != two) {
+      printf("FAIL base-2 round n=%llu\n", n);
+      return 1;
     }
   }
   for (int bits = 18; bits <= 31; ++bits) {
