@@ -692,11 +692,16 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
   const U128 INF{~0ull, ~0ull};
   const ModR R(r);
   const u32 one = r == 1 ? 0u : 1u;              // 1 mod r
-  for (u32 t = lane; t < r; t += 32) D.cur[t] = (t == one) ? U128{1, 0} : INF;
+  // p's own stage: q = pA with A < p, so p^2 > q and p enters with exponent 0 or 1 -- the
+  // divisors 1 and p (this one only when p is within the bound)
+  const u32 pm = R.mod64(p);
+  const bool p_fits = !lt128(q, U128{p, 0});
+  for (u32 t = lane; t < r; t += 32)
+    D.cur[t] = (t == one) ? U128{1, 0} : (p_fits && t == pm) ? U128{p, 0} : INF;
   __syncwarp();
-  for (int idx = -1; idx < F.k; ++idx) {
-    const u64 pr = idx < 0 ? p : F.pr[idx];
-    const int e = idx < 0 ? 2 : 2 * (int)F.ex[idx];
+  for (int idx = 0; idx < F.k; ++idx) {
+    const u64 pr = F.pr[idx];
+    const int e = 2 * (int)F.ex[idx];
     const u32 prm = R.mod64(pr);
     u32 inv = 0;                                 // prm^-1 mod r (prm is a unit: gcd(q, r) = 1)
     for (u32 base = 0; base < r; base += 32) {
