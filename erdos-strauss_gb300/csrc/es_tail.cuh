@@ -662,9 +662,8 @@ __device__ __forceinline__ bool mul_le128(U128 a, U128 b, U128 q, U128 &out) {
   return !over && !lt128(q, out);
 }
 
-struct DPWarp {            // shared memory, one per warp
-  U128 cur[RCAP + 1];
-  U128 nxt[RCAP + 1];
+struct DPWarp {            // shared memory, one per warp: the DP's table and the next one, in turn
+  U128 v[2][RCAP + 1];
 };
 
 // Residues modulo a rung's r (1 <= r <= RCAP) without a division per residue: Barrett
@@ -696,8 +695,9 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
   // divisors 1 and p (this one only when p is within the bound)
   const u32 pm = R.mod64(p);
   const bool p_fits = !lt128(q, U128{p, 0});
+  u32 ph = 0;                                     // D.v[ph] is the current table
   for (u32 t = lane; t < r; t += 32)
-    D.cur[t] = (t == one) ? U128{1, 0} : (p_fits && t == pm) ? U128{p, 0} : INF;
+    D.v[0][t] = (t == one) ? U128{1, 0} : (p_fits && t == pm) ? U128{p, 0} : INF;
   __syncwarp();
   for (int idx = 0; idx < F.k; ++idx) {
     const u64 pr = F.pr[idx];
@@ -720,18 +720,17 @@ __device__ inline U128 warp_min_div_res(u64 p, const WarpFac &F, U128 q, u32 r, 
           if (over || lt128(q, pw)) break;       // pr^j > q: nothing further fits
           s = R.mod32(s * inv);
         }
-        const U128 v = D.cur[s];
+        const U128 v = D.v[ph][s];
         if (v.lo == ~0ull && v.hi == ~0ull) continue;
         U128 cand;
         if (mul_le128(v, pw, q, cand) && lt128(cand, best)) best = cand;
       }
-      D.nxt[t] = best;
+      D.v[ph ^ 1][t] = best;
     }
-    __syncwarp();
-    for (u32 t = lane; t < r; t += 32) D.cur[t] = D.nxt[t];
-    __syncwarp();
+    __syncwarp();                                  // every lane has read D.v[ph]: swap
+    ph ^= 1;
   }
-  const U128 u = D.cur[target];
+  const U128 u = D.v[ph][target];
   __syncwarp();
   return (u.lo == ~0ull && u.hi == ~0ull) ? U128{0, 0} : u;
 }
