@@ -119,12 +119,23 @@ struct ItemInfo {
 
 // Per-window residues (lo / M) mod s_d for every distinct stride: computed once per window
 // here, instead of once per (window, lane) item.
+// Qm[w][d] = Q_w mod s_d. A thread keeps its strides d = threadIdx.x + k blockDim over the
+// block's windows, with the Barrett constant of each stride taken once: Q < 2^64 / M, so Q mod
+// s for s < 2^16 is three 16-bit steps of a 32-bit reduction (the quotient estimate
+// umulhi(x, m), m = floor((2^32 - 1) / s), is low by at most one).
 __global__ void k_prep(const BatchHdr *__restrict__ hdr, const WinDev *__restrict__ win,
                        const u32 *__restrict__ sdist, u32 D, u32 Dq, u16 *__restrict__ Qm) {
-  const u64 total = (u64)hdr->nwin * D;
-  for (u64 idx = (u64)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (u64)gridDim.x * blockDim.x) {
-    const u32 w = (u32)(idx / D), d = (u32)(idx % D);
-    Qm[(size_t)w * Dq + d] = (u16)(win[w].Q % sdist[d]);
+  const u32 nwin = hdr->nwin;
+  for (u32 d = threadIdx.x; d < D; d += blockDim.x) {
+    const u32 sd = sdist[d], m = 0xFFFFFFFFu / sd;
+    auto mod = [&](u32 x) { const u32 v = x - __umulhi(x, m) * sd; return v >= sd ? v - sd : v; };
+    for (u32 w = blockIdx.x; w < nwin; w += gridDim.x) {
+      const u64 Q = win[w].Q;
+      u32 r = mod((u32)(Q >> 32));
+      r = mod((r << 16) | ((u32)(Q >> 16) & 0xFFFFu));
+      r = mod((r << 16) | ((u32)Q & 0xFFFFu));
+      Qm[(size_t)w * Dq + d] = (u16)r;
+    }
   }
 }
 
