@@ -53,9 +53,9 @@ MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
     (128, 1): {"inst": 745716421, "dram": 95081216 + 3645440},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
-    4: {"inst": 79429266, "dram": 853248},
-    6: {"inst": 79412528, "dram": 852736},
-    8: {"inst": 79795257, "dram": 850176},
+    4: {"inst": 72291376, "dram": 850944 + 256},
+    6: {"inst": 72331788, "dram": 849152},
+    8: {"inst": 72584942, "dram": 849920},
 }
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
