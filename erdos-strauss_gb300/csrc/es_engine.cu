@@ -42,6 +42,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cinttypes>
 #include <condition_variable>
@@ -327,6 +328,9 @@ __device__ __forceinline__ u32 warp_or32(u32 v) { return __reduce_or_sync(0xFFFF
 // as nothing is left alive: the strides come densest first, so most segments are dead after
 // one or two rounds. Returns nonzero if a position is still alive.
 
+#ifndef ES_FIRST_SH
+#define ES_FIRST_SH 1
+#endif
 template <int NC>
 __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], const u32 (&b)[SHORT_LANES],
                                                  const u32 *tab, u32 tab_words, const MaskDesc *smd, u32 m0,
@@ -339,21 +343,31 @@ __device__ __forceinline__ u32 short_mask_rounds(u32 (&alive)[SHORT_LANES][NC], 
   u32 q0 = k + 32 < m1 ? (u32)__ldg(Qrow + smd[k + 32].d) : 0u;    // the next round's residue
   if (k < m1) {
     const MaskDesc md = md_first;                    // this lane's stride of the first round
-    #pragma unroll
-    for (int q = 0; q < SHORT_LANES; ++q) {
-      u32 r = q0_first + b[q];
-      r = r >= md.s ? r - md.s : r;
-      // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
-      const u32 *wp = tab + q * tab_words + md.off + ((r >> 5) << md.sh);
-      const u32 sh = r & 31;
-      u32 w0 = wp[0];
+    // SH: the round's row layout (the same for all its strides), a constant in each copy
+    auto first = [&](auto shc) {
+      constexpr u32 SH = decltype(shc)::value;
+      u32 r = 0;
       #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const u32 w1 = wp[(c + 1) << md.sh];
-        kill[q][c] = __funnelshift_r(w0, w1, sh);
-        w0 = w1;
+      for (int q = 0; q < SHORT_LANES; ++q) {
+        if (q == 0 || b[q] != b[0]) {                // lanes whose segments start together share r
+          r = q0_first + b[q];
+          r = r >= md.s ? r - md.s : r;
+        }
+        // the mask repeats for SEG_SMALL bits past s, so chunk c is words r/32 + c, + c + 1
+        const u32 *wp = tab + q * tab_words + md.off + ((r >> 5) << (SH == 1 ? md.sh : SH));
+        const u32 sh = r & 31;
+        u32 w0 = wp[0];
+        #pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          const u32 w1 = wp[(c + 1) << (SH == 1 ? md.sh : SH)];
+          kill[q][c] = __funnelshift_r(w0, w1, sh);
+          w0 = w1;
+        }
       }
-    }
+    };
+    if (!ES_FIRST_SH) first(std::integral_constant<u32, 1>{});   // 1: the layout read at run time
+    else if (md.sh == 5) first(std::integral_constant<u32, 5>{});
+    else first(std::integral_constant<u32, 0>{});
   } else {
     #pragma unroll
     for (int q = 0; q < SHORT_LANES; ++q)
