@@ -48,9 +48,9 @@ METRIC = "verified integers/s at 1e19 (batched vs plain, 1 GB300)"
 # k_mark_short's depend on (short_max, long_split), k_rung's on rung_blocks_per_sm. A schedule
 # with no capture here gets no issue figure rather than another schedule's.
 MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
-    (32, 1): {"inst": 734442333, "dram": 95898880 + 3676672},
-    (64, 1): {"inst": 724482591, "dram": 95406336 + 3820288},
-    (128, 1): {"inst": 745716421, "dram": 95081216 + 3645440},
+    (32, 1): {"inst": 728342167, "dram": 95922688 + 3819776},
+    (64, 1): {"inst": 718216590, "dram": 95236608 + 3364864},
+    (128, 1): {"inst": 735127673, "dram": 95047680 + 3439104},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
     4: {"inst": 72291376, "dram": 850944 + 256},
