@@ -6,13 +6,17 @@
 // lane without a collision: in practice a product of two primes of 24-31 bits. For those the
 // expected rho walk grows like the square root of the smaller prime (about 20 K steps, 40 K
 // Montgomery multiplies, for two 31-bit primes, over 32 walks in lockstep), while one ECM
-// curve with B1 = 40 and B2 = 2000 costs about 1.3 K multiplies and succeeds with probability
-// ~0.02 for a 31-bit prime, ~0.15 for a 24-bit one: a round of 32 curves in a warp splits a
-// 31-bit pair about half the time, a 24-bit one almost always. On GB300 a single warp's
-// multiply chain is latency-bound (about 0.1 us per 64-bit Montgomery multiply), so short
-// rounds that fail now and then beat long sure ones: measured on the 4096-window batch, stage D
-// took 0.45 ms with B1 = 40, 0.47 with 50, 0.48 with 60, 0.55 with 85 and 0.49 with 30, whose
-// 2^34 window at 1.8e19 then needed 2.1 ms (too many failed rounds). The reference factors
+// curve with B1 = 40 and B2 = 1200 costs about 1.25 K multiplies and splits a 31-bit prime
+// with a probability of about 0.015, a 24-bit one about 0.12: a round of 32 curves in a warp
+// splits a 31-bit pair about a third of the time, a 24-bit one almost always, and block-mates
+// add rounds of their own. On GB300 a single warp's multiply chain is latency-bound (about
+// 0.1 us per 64-bit Montgomery multiply), so short rounds that fail now and then beat long sure
+// ones: measured on the 4096-window batch, stage D took 0.45 ms with B1 = 40, 0.47 with 50,
+// 0.48 with 60, 0.55 with 85 and 0.49 with 30, whose 2^34 window at 1.8e19 then needed 2.1 ms
+// (too many failed rounds); with B1 = 40 and the curves inversion-free, B2 = 1200 against
+// 2000 and 3000: 0.34 against 0.36 and 0.41 ms here, 0.56-0.58 against 0.59-0.60 and
+// 0.62-0.63 ms on the batch at 1e19, 0.32 against 0.35-0.36 and 0.39-0.40 ms on that 2^34
+// window (B2 = 800 measured within noise of 1200). The reference factors
 // with rho alone (sieve/rung_scan3.cpp:333-369); the factorization of a number is unique, so
 // the method that finds a divisor cannot change any certificate.
 //
@@ -38,7 +42,7 @@
 namespace es {
 
 constexpr u32 ECM_B1 = 40;
-constexpr u32 ECM_B2 = 2000;
+constexpr u32 ECM_B2 = 1200;
 constexpr u32 ECM_D = 60;
 // k = lcm(1..40) = prod over primes p <= 40 of p^floor(log_p 40): 53 bits, little-endian words.
 constexpr int ECM_K_BITS = 53;
@@ -48,14 +52,13 @@ constexpr int ECM_NJ = 8;
 __constant__ const u32 ECM_J[ECM_NJ] = {1, 7, 11, 13, 17, 19, 23, 29};
 // Giant steps m = 1 .. ECM_M1 (ECM_M1 = floor((B2 + D/2) / D)); bit i of ECM_PAIRS[m - 1] is set
 // when m*D + J[i] or m*D - J[i] is a prime in (B1, B2]. Every prime of (B1, B2] is covered.
-constexpr int ECM_M1 = 33;
+constexpr int ECM_M1 = 20;
 __constant__ const unsigned char ECM_PAIRS[ECM_M1] = {
     0xff, 0xfe, 0xff, 0xdf, 0xfe, 0xef, 0xed, 0xff, 0xf3, 0xfb, 0xfb, 0xef, 0xf6, 0xfd, 0xfe, 0x7e,
-    0xef, 0xfe, 0x5c, 0xfb, 0xf5, 0xfb, 0xab, 0x3f, 0xff, 0xf7, 0x7f, 0xfc, 0x3b, 0x5d, 0xbf, 0xae,
-    0xbb};
-// One round (about 1.6 K Montgomery multiplies: 12 per bit of k, 3 per stage-2 pair, 6 per
-// giant step) in rho steps of two multiplies.
-constexpr u64 ECM_ROUND_STEPS = 800;
+    0xef, 0xfe, 0x5c, 0xaa};
+// One round (about 1.25 K Montgomery multiplies: 12 per bit of k, 3 per stage-2 pair, 6 per
+// giant step and baby step) in rho steps of two multiplies.
+constexpr u64 ECM_ROUND_STEPS = 625;
 
 struct XZ { u64 x, z; };
 

@@ -225,7 +225,7 @@ __device__ inline u64 warp_ecm(const Mont &M, u64 sigma0, u32 lane, Poll poll, u
 #define ES_ECM_AFTER 512
 #endif
 constexpr u64 ECM_AFTER = ES_ECM_AFTER;
-constexpr u32 ECM_OWNER_ROUNDS = 32;     // 1024 curves: a 31-bit factor survives them w.p. ~1e-9
+constexpr u32 ECM_OWNER_ROUNDS = 32;     // 1024 curves: a 31-bit factor survives them w.p. ~2e-7
 constexpr u64 ECM_SIGMA_OWNER = 6;       // owner round r: sigma = 6 + 32 r + lane
 constexpr u64 ECM_SIGMA_HELP = 4096;     // helper session t: sigma = 4096 + 32 t + lane
 constexpr u64 ECM_SIGMA_LOCAL = 1ull << 22;   // block-mate session t: sigma = 2^22 + 32 t + lane
