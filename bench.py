@@ -53,9 +53,9 @@ MARK_SHORT_NCU = {            # (short_max, long_split) -> per launch
     (128, 1): {"inst": 735127673, "dram": 95047680 + 3439104},
 }
 RUNG_NCU = {                  # rung_blocks_per_sm -> per launch
-    4: {"inst": 72291376, "dram": 850944 + 256},
-    6: {"inst": 72331788, "dram": 849152},
-    8: {"inst": 72584942, "dram": 849920},
+    4: {"inst": 70295758, "dram": 845824 + 768},
+    6: {"inst": 70433215, "dram": 845824},
+    8: {"inst": 70539276, "dram": 846592},
 }
 # Cover/filter marks per integer of the 2042040 wheel with the gpu filter table: 9.0951 marks per
 # position (positions of all 2308 lanes, all 3745 filters) over 2042040 / 2308 integers per position.
