@@ -16,7 +16,9 @@
 // (too many failed rounds); with B1 = 40 and the curves inversion-free, B2 = 1200 against
 // 2000 and 3000: 0.34 against 0.36 and 0.41 ms here, 0.56-0.58 against 0.59-0.60 and
 // 0.62-0.63 ms on the batch at 1e19, 0.32 against 0.35-0.36 and 0.39-0.40 ms on that 2^34
-// window (B2 = 800 measured within noise of 1200). The reference factors
+// window (B2 = 800 measured within noise of 1200); B1 re-checked with B2 = 1200: 30 lost at 1e19
+// (0.69-0.76 against 0.54-0.56 ms), 50 gained there what it lost on the 4096-window batch
+// (0.53-0.54 against 0.54-0.56, and 0.35-0.37 against 0.34-0.35 ms). The reference factors
 // with rho alone (sieve/rung_scan3.cpp:333-369); the factorization of a number is unique, so
 // the method that finds a divisor cannot change any certificate.
 //
