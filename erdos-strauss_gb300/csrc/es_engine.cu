@@ -780,6 +780,12 @@ constexpr int RUNG_WARPS = ES_RUNG_WARPS;
 #ifndef ES_HELP_BLOCKS_PER_SM
 #define ES_HELP_BLOCKS_PER_SM 1
 #endif
+#ifndef ES_FEW_ECM_DIV
+#define ES_FEW_ECM_DIV 4
+#endif
+#ifndef ES_FEW_ECM_AFTER
+#define ES_FEW_ECM_AFTER 384
+#endif
 #ifndef ES_HELP_FEW_DIV
 #define ES_HELP_FEW_DIV 16
 #endif
@@ -825,6 +831,9 @@ __global__ void __launch_bounds__(RUNG_WARPS * 32, ES_RUNG_MIN_BLOCKS) k_rung(co
   HardBoard B;
   B.slot = T.board; B.sessions = T.help_sessions; B.done = T.rung_done; B.total = n;
   B.local = nullptr;                                 // the warp phase: no block-mates on one prime
+  // A run of few primes is bound by the latency of its hardest factorizations, on SMs that are
+  // otherwise idle: its cofactors turn to curves sooner.
+  B.ecm_after = (ES_FEW_ECM_DIV && n * ES_FEW_ECM_DIV <= (u64)gridDim.x) ? ES_FEW_ECM_AFTER : 0;
   const u64 tail = min(n, (u64)gridDim.x * ES_RUNG_TAIL_PER_BLOCK);
   const u64 nw = n - tail;                           // primes [0, nw): a warp each
   for (;;) {

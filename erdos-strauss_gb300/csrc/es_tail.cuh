@@ -154,6 +154,7 @@ struct HardBoard {
   unsigned long long *done;                    // primes finished by k_rung
   unsigned long long total;                    // primes k_rung has to finish
   BlockHelp *local;                            // the block's own slot, or null
+  u64 ecm_after;                               // rho steps per lane before curves (0: ECM_AFTER)
 };
 
 __device__ __forceinline__ u64 ld_volatile(const unsigned long long *p) { return *(const volatile unsigned long long *)p; }
@@ -289,10 +290,11 @@ __device__ inline u64 warp_rho(u64 n, u32 lane, volatile u64 *found, u32 *status
   if (n >= LazyArith::NMAX) {
     f = rho_walk<ExactArith>(n, M, 1 + lane, 32, budget, lane, poll);
   } else {
-    const bool ecm = use_ecm && budget >= ECM_AFTER + ECM_ROUND_STEPS;
-    f = rho_walk<LazyArith>(n, M, 1 + lane, 32, ecm ? ECM_AFTER : budget, lane, poll);
+    const u64 after = board && board->ecm_after ? board->ecm_after : ECM_AFTER;
+    const bool ecm = use_ecm && budget >= after + ECM_ROUND_STEPS;
+    f = rho_walk<LazyArith>(n, M, 1 + lane, 32, ecm ? after : budget, lane, poll);
     if (!f && !stop && ecm) {
-      u64 steps = ECM_AFTER;
+      u64 steps = after;
       u64 ext = poll(RHO_POST_STEPS > steps ? RHO_POST_STEPS : steps);   // post n to the board now
       if (ext && ext != ~0ull) f = ext;
       for (u32 round = 0; !f && !stop && round < ECM_OWNER_ROUNDS && steps + ECM_ROUND_STEPS <= budget; ++round) {
